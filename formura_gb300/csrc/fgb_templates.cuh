@@ -1,0 +1,224 @@
+// Hand-written sm_103a kernel templates.  Each program's step function is
+// emitted as one functor per stage (see formura_gb300/generator/cuda.py);
+// these templates supply the arithmetic policy, the storage format, the
+// periodic in-kernel wrap that replaces the reference's halo exchange
+// (Functions.hs:265-307, Templates.hs:336-346) and the launch geometry.
+#pragma once
+#include <cuda_runtime.h>
+#include <cuda_fp16.h>
+#include <stdint.h>
+#include "fgb_internal.h"
+
+namespace fgb {
+
+// ---------------------------------------------------------------------------
+// arithmetic policies
+// ---------------------------------------------------------------------------
+// FP64, rounding exactly like the reference's C: one IEEE rounding per SSA
+// operation, no contraction (the __d*_rn intrinsics are never fused).
+struct F64Exact {
+  using T = double;
+  static __device__ __forceinline__ T add(T a, T b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ T sub(T a, T b) { return __dsub_rn(a, b); }
+  static __device__ __forceinline__ T mul(T a, T b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ T div(T a, T b) { return __ddiv_rn(a, b); }
+  // a*b + c where a*b is exact (a is a power of two): same result as the
+  // separately rounded product and sum.
+  static __device__ __forceinline__ T fma(T a, T b, T c) { return __fma_rn(a, b, c); }
+  // x / c for a grid-independent c with rc = RN(1/c): Markstein's
+  // correction step gives the correctly rounded quotient.
+  static __device__ __forceinline__ T divu(T x, T c, T rc) {
+#ifdef FGB_DIVU_IEEE
+    (void)rc;
+    return __ddiv_rn(x, c);
+#else
+    const T q = __dmul_rn(x, rc);
+    const T e = __fma_rn(-q, c, x);
+    return __fma_rn(e, rc, q);
+#endif
+  }
+  static __device__ __forceinline__ T neg(T a) { return -a; }
+  static __device__ __forceinline__ T sqrt(T a) { return __dsqrt_rn(a); }
+  static __device__ __forceinline__ T fabs(T a) { return ::fabs(a); }
+  static __device__ __forceinline__ T exp(T a) { return ::exp(a); }
+  static __device__ __forceinline__ T log(T a) { return ::log(a); }
+  static __device__ __forceinline__ T sin(T a) { return ::sin(a); }
+  static __device__ __forceinline__ T cos(T a) { return ::cos(a); }
+  static __device__ __forceinline__ T pow(T a, T b) { return ::pow(a, b); }
+};
+
+// FP64 with contraction and reciprocal multiplication (not bit-faithful).
+struct F64Fast {
+  using T = double;
+  static __device__ __forceinline__ T add(T a, T b) { return a + b; }
+  static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
+  static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
+  static __device__ __forceinline__ T div(T a, T b) { return a / b; }
+  static __device__ __forceinline__ T fma(T a, T b, T c) { return ::fma(a, b, c); }
+  static __device__ __forceinline__ T divu(T x, T, T rc) { return x * rc; }
+  static __device__ __forceinline__ T neg(T a) { return -a; }
+  static __device__ __forceinline__ T sqrt(T a) { return ::sqrt(a); }
+  static __device__ __forceinline__ T fabs(T a) { return ::fabs(a); }
+  static __device__ __forceinline__ T exp(T a) { return ::exp(a); }
+  static __device__ __forceinline__ T log(T a) { return ::log(a); }
+  static __device__ __forceinline__ T sin(T a) { return ::sin(a); }
+  static __device__ __forceinline__ T cos(T a) { return ::cos(a); }
+  static __device__ __forceinline__ T pow(T a, T b) { return ::pow(a, b); }
+};
+
+// FP32 arithmetic (used with float or half storage).
+struct F32 {
+  using T = float;
+  static __device__ __forceinline__ T add(T a, T b) { return a + b; }
+  static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
+  static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
+  static __device__ __forceinline__ T div(T a, T b) { return a / b; }
+  static __device__ __forceinline__ T fma(T a, T b, T c) { return fmaf(a, b, c); }
+  static __device__ __forceinline__ T divu(T x, T, T rc) { return x * rc; }
+  static __device__ __forceinline__ T neg(T a) { return -a; }
+  static __device__ __forceinline__ T sqrt(T a) { return sqrtf(a); }
+  static __device__ __forceinline__ T fabs(T a) { return fabsf(a); }
+  static __device__ __forceinline__ T exp(T a) { return expf(a); }
+  static __device__ __forceinline__ T log(T a) { return logf(a); }
+  static __device__ __forceinline__ T sin(T a) { return sinf(a); }
+  static __device__ __forceinline__ T cos(T a) { return cosf(a); }
+  static __device__ __forceinline__ T pow(T a, T b) { return powf(a, b); }
+};
+
+// ---------------------------------------------------------------------------
+// storage formats of the state
+// ---------------------------------------------------------------------------
+template <class S, class T> struct Storage;
+template <> struct Storage<double, double> {
+  static __device__ __forceinline__ double load(double s, float) { return s; }
+  static __device__ __forceinline__ double store(double v, float) { return v; }
+};
+template <> struct Storage<float, float> {
+  static __device__ __forceinline__ float load(float s, float) { return s; }
+  static __device__ __forceinline__ float store(float v, float) { return v; }
+};
+// half storage with a per-field scale: value = half * scale
+template <> struct Storage<__half, float> {
+  static __device__ __forceinline__ float load(__half s, float scale) { return __half2float(s) * scale; }
+  static __device__ __forceinline__ __half store(float v, float inv_scale) {
+    return __float2half_rn(v * inv_scale);
+  }
+};
+
+// precision index -> (policy, storage)
+template <int P> struct Precision;
+template <> struct Precision<0> { using M = F64Exact; using S = double; };
+template <> struct Precision<1> { using M = F64Fast; using S = double; };
+template <> struct Precision<2> { using M = F32; using S = float; };
+template <> struct Precision<3> { using M = F32; using S = __half; };
+
+// ---------------------------------------------------------------------------
+// periodic index arithmetic (in-kernel wrap instead of halo buffers)
+// ---------------------------------------------------------------------------
+template <int D>
+__device__ __forceinline__ int wrap(int p, int n) {
+  if constexpr (D == 0) {
+    return p;
+  } else if constexpr (D > 0) {
+    const int i = p + D;
+    return i >= n ? i - n : i;
+  } else {
+    const int i = p + D;
+    return i < 0 ? i + n : i;
+  }
+}
+
+// Accessor of the generic stage kernel: global loads at p + D, stores of the
+// new state at p + shift (the reference's per-step roll, Templates.hs:346).
+template <class S, class T, int DIM, int SHIFT>
+struct GlobalAccess {
+  const FgbLaunch& L;
+  int p0, p1, p2;
+
+  __device__ __forceinline__ uint32_t lin(int i0, int i1, int i2) const {
+    return ((uint32_t)i0 * (uint32_t)L.n[1] + (uint32_t)i1) * (uint32_t)L.n[2] + (uint32_t)i2;
+  }
+  template <int F, int D0, int D1, int D2>
+  __device__ __forceinline__ T ld() const {
+    const S* a = static_cast<const S*>(L.in[F]);
+    const uint32_t k = lin(wrap<D0>(p0, L.n[0]), wrap<D1>(p1, L.n[1]), wrap<D2>(p2, L.n[2]));
+    return Storage<S, T>::load(a[k], L.scale[F]);
+  }
+  template <int K, int D0, int D1, int D2>
+  __device__ __forceinline__ T ldm() const {
+    const T* a = static_cast<const T*>(L.mid[K]);
+    return a[lin(wrap<D0>(p0, L.n[0]), wrap<D1>(p1, L.n[1]), wrap<D2>(p2, L.n[2]))];
+  }
+  template <int F>
+  __device__ __forceinline__ void st(T v) const {
+    S* a = static_cast<S*>(L.out[F]);
+    const int i0 = DIM >= 3 ? wrap<SHIFT>(p0, L.n[0]) : p0;
+    const int i1 = DIM >= 2 ? wrap<SHIFT>(p1, L.n[1]) : p1;
+    const int i2 = wrap<SHIFT>(p2, L.n[2]);
+    a[lin(i0, i1, i2)] = Storage<S, T>::store(v, L.inv_scale[F]);
+  }
+  template <int K>
+  __device__ __forceinline__ void stm(T v) const {
+    static_cast<T*>(L.mid[K])[lin(p0, p1, p2)] = v;
+  }
+};
+
+constexpr int kBlockX = 128;
+
+// One thread per grid point; x covers the contiguous (last) axis.
+template <class M, class S, int DIM, int SHIFT, class Stage>
+__global__ void __launch_bounds__(kBlockX) stage_kernel(const __grid_constant__ FgbLaunch L) {
+  const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p2 >= L.n[2]) return;
+  GlobalAccess<S, typename M::T, DIM, SHIFT> a{L, (int)blockIdx.z, (int)blockIdx.y, p2};
+  Stage::template run<M>(a, static_cast<const typename M::T*>(L.uniforms));
+}
+
+template <class Prog, int P, class Stage>
+cudaError_t launch_stage(const FgbLaunch* L, cudaStream_t stream) {
+  using M = typename Precision<P>::M;
+  using S = typename Precision<P>::S;
+  const int bx = L->n[2] >= kBlockX ? kBlockX : ((L->n[2] + 31) / 32) * 32;
+  dim3 grid((L->n[2] + bx - 1) / bx, L->n[1], L->n[0]);
+  stage_kernel<M, S, Prog::kDim, Prog::kShift, Stage><<<grid, bx, 0, stream>>>(*L);
+  return cudaGetLastError();
+}
+
+template <class Prog, class... Stages>
+struct ProgramBuilder {
+  template <int P>
+  static void fill(FgbProgramDesc& d) {
+    FgbStageLaunch l[] = {&launch_stage<Prog, P, Stages>...};
+    for (int i = 0; i < (int)sizeof...(Stages); ++i) d.launch[P][i] = l[i];
+  }
+  static FgbProgramDesc make(const char* name, const char* const* fields) {
+    static_assert(sizeof...(Stages) == Prog::kStages, "stage count");
+    static_assert(Prog::kStages <= FGB_MAX_STAGES, "too many stages");
+    static_assert(Prog::kFields <= FGB_MAX_FIELDS, "too many fields");
+    static_assert(Prog::kMids <= FGB_MAX_MIDS, "too many intermediate arrays");
+    FgbProgramDesc d = {};
+    d.name = name;
+    d.dim = Prog::kDim;
+    d.nfields = Prog::kFields;
+    d.nmids = Prog::kMids;
+    d.nstages = Prog::kStages;
+    d.sleeve = Prog::kSleeve;
+    d.shift = Prog::kShift;
+    d.reach = Prog::kReach;
+    d.nuniforms = Prog::kUniforms;
+    d.field_names = fields;
+    fill<0>(d);
+    fill<1>(d);
+    fill<2>(d);
+    fill<3>(d);
+    return d;
+  }
+};
+
+}  // namespace fgb
+
+#define FGB_DEFINE_PROGRAM(NAME, PROG, FIELDS, ...)                                   \
+  extern "C" const FgbProgramDesc* fgb_program_##NAME(void) {                         \
+    static const FgbProgramDesc d = fgb::ProgramBuilder<PROG, __VA_ARGS__>::make(#NAME, FIELDS); \
+    return &d;                                                                         \
+  }

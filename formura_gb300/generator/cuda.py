@@ -1,0 +1,568 @@
+"""CUDA emission: turns a program's step graph (Manifest Machine) into the
+device code that the hand-written sm_103a kernel templates of
+``formura_gb300/csrc/fgb_templates.cuh`` are instantiated with.
+
+Where the reference emits one OpenMP loop nest per manifest node over a
+halo-padded buffer (``src/Formura/Generator/Templates.hs:426-487``), this
+backend groups manifest nodes into *stages*.  A node joins the stage of a
+dependency it reads only at cursor 0 (the value stays in registers), and opens
+a later stage when it reads a dependency at a nonzero cursor (the value goes
+through an HBM array).  Heat and Gray-Scott are one stage; HLLC/HLLD are
+three.  Loads wrap periodically in-kernel instead of reading a halo buffer.
+
+Arithmetic follows the reference's SSA chain one operation at a time, so the
+FP64 form rounds exactly where the reference's C rounds:
+
+* subexpressions that do not depend on the grid (``dt``, ``dx**2`` ...) are
+  evaluated once on the host, each operation correctly rounded, which is what
+  gcc's constant folding of the reference's literal chain gives;
+* ``pow(x, 2)`` is ``x*x`` (gcc expands it the same way); ``sqrt`` is
+  correctly rounded on both sides;
+* a product by a literal power of two is exact, so ``a - 2*b`` may become one
+  fused multiply-add without changing the result;
+* division by a grid-independent value uses the reciprocal and one fused
+  correction step (Markstein's theorem: with ``r = RN(1/c)``, ``q = RN(x*r)``,
+  ``e = fma(-q, c, x)``, ``RN(q + e*r)`` is the correctly rounded ``x/c``);
+  the policy selects it only after the GPU self-check in the tests.
+"""
+from __future__ import annotations
+
+import math
+import struct
+from dataclasses import dataclass, field
+from decimal import Decimal, localcontext
+from fractions import Fraction
+from typing import Dict, List, Optional, Set, Tuple
+
+from .manifest import MMNode, MMProgram, MicroNode, calc_range
+from .translate import FormuraCompileError
+
+
+# --------------------------------------------------------------------------
+# correctly rounded evaluation of grid-independent values
+# --------------------------------------------------------------------------
+def _dec(x: float) -> Decimal:
+    return Decimal(Fraction(x).numerator) / Decimal(Fraction(x).denominator)
+
+
+def _dec_sin(x: Decimal) -> Decimal:
+    with localcontext() as ctx:
+        ctx.prec += 10
+        two_pi = Decimal("6.283185307179586476925286766559005768394338798750211641949889184615632812572417997")
+        x = x % two_pi
+        term, s, k = x, x, 1
+        while True:
+            term = -term * x * x / ((2 * k) * (2 * k + 1))
+            if abs(term) < Decimal(10) ** (-(ctx.prec + 5)):
+                break
+            s += term
+            k += 1
+    return +s
+
+
+def external_value(f: str, x: float) -> float:
+    """Correctly rounded libm function of a constant (what gcc folds to)."""
+    if f == "sqrt":
+        return math.sqrt(x)
+    if f == "fabs":
+        return abs(x)
+    with localcontext() as ctx:
+        ctx.prec = 60
+        d = _dec(x)
+        if f == "exp":
+            return float(d.exp())
+        if f == "log":
+            return float(d.ln())
+        if f == "sin":
+            return float(_dec_sin(d))
+        if f == "cos":
+            return float(_dec_sin(d + Decimal("1.5707963267948966192313216916397514420985846996875529104874722961539082031431044993")))
+    raise FormuraCompileError(f"external function {f} has no host evaluation")
+
+
+def pow_value(a: float, b: float) -> float:
+    if b == int(b) and abs(b) <= 64:
+        n = int(b)
+        if a == 0.0:
+            return math.pow(a, b)
+        v = Fraction(a) ** n
+        return float(v)
+    with localcontext() as ctx:
+        ctx.prec = 60
+        return float((_dec(b) * _dec(a).ln()).exp())
+
+
+def fold(inst, vals) -> object:
+    """Evaluate one micro instruction on constant operands (IEEE double)."""
+    k = inst[0]
+    if k == "imm":
+        return float(inst[1])
+    if k == "uniop":
+        op, a = inst[1], vals[0]
+        if op == "-":
+            return -a
+        if op == "+":
+            return a
+        if op.startswith("external-call/"):
+            return external_value(op[len("external-call/"):], a)
+        raise FormuraCompileError(f"unary operator {op}")
+    if k == "binop":
+        op, a, b = inst[1], vals[0], vals[1]
+        if op == "+":
+            return a + b
+        if op == "-":
+            return a - b
+        if op == "*":
+            return a * b
+        if op == "/":
+            return a / b if b != 0 else math.copysign(math.inf, a) * math.copysign(1, b)
+        if op == "**":
+            return pow_value(a, b)
+        if op == "<":
+            return a < b
+        if op == ">":
+            return a > b
+        if op == "<=":
+            return a <= b
+        if op == ">=":
+            return a >= b
+        if op == "==":
+            return a == b
+        if op == "!=":
+            return a != b
+        if op == "&&":
+            return bool(a) and bool(b)
+        if op == "||":
+            return bool(a) or bool(b)
+        raise FormuraCompileError(f"binary operator {op}")
+    if k == "triop":
+        return vals[1] if vals[0] else vals[2]
+    raise FormuraCompileError(f"cannot fold {k}")
+
+
+def c_double(x: float) -> str:
+    """Exact C literal for a double."""
+    if x != x:
+        return "(0.0/0.0)"
+    if math.isinf(x):
+        return "(1.0/0.0)" if x > 0 else "(-1.0/0.0)"
+    return float.hex(x)
+
+
+def is_pow2(x: float) -> bool:
+    if x == 0 or not math.isfinite(x):
+        return False
+    m, _ = math.frexp(abs(x))
+    return m == 0.5
+
+
+# --------------------------------------------------------------------------
+# program analysis
+# --------------------------------------------------------------------------
+CONFIG_NAMES_PREFIX = ("total_grid_",)
+
+
+@dataclass
+class Stage:
+    index: int
+    nodes: List[MMNode]
+    writes_state: bool
+    mid_out: List[int] = field(default_factory=list)   # manifest ids stored to HBM
+
+
+@dataclass
+class KernelProgram:
+    name: str
+    dim: int
+    axes: List[str]
+    fields: List[str]
+    sleeve: int
+    shift: int                   # output index = position + shift (periodic)
+    max_reach: int               # largest |cursor| read from any array
+    stages: List[Stage]
+    mids: List[int]              # manifest ids stored to HBM, in array order
+    uniform_exprs: List[tuple]   # table entries: ('node', key) evaluated by host
+    runtime_params: List[str]
+    source: str = ""             # generated CUDA
+
+
+class _Analysis:
+    """Classifies micro nodes of one program: grid-independent (uniform) or
+    not, and whether a uniform value depends on the configuration."""
+
+    def __init__(self, mm: MMProgram, runtime_params: List[str]):
+        self.mm = mm
+        self.g = mm.om.step_graph
+        self.axes = mm.om.genv.axes
+        names = {"d" + a for a in self.axes} | {"total_grid_" + a for a in self.axes}
+        names |= set(runtime_params)
+        self.param_names = names
+        self._uni: Dict[int, bool] = {}
+        self._cfg: Dict[int, bool] = {}
+
+    def om_uniform(self, nid: int) -> bool:
+        """An OM node is uniform when no grid load reaches it."""
+        if nid in self._uni:
+            return self._uni[nid]
+        inst = self.g[nid].inst
+        k = inst[0]
+        if k == "imm":
+            r = True
+        elif k in ("uniop",):
+            r = self.om_uniform(inst[2])
+        elif k == "binop":
+            r = self.om_uniform(inst[2]) and self.om_uniform(inst[3])
+        elif k == "triop":
+            r = all(self.om_uniform(x) for x in inst[2:5])
+        elif k == "shift":
+            r = self.om_uniform(inst[2])
+        else:
+            r = False
+        self._uni[nid] = r
+        return r
+
+    def om_config_dependent(self, nid: int) -> bool:
+        """A uniform node whose value changes with the numerical config or a
+        runtime parameter (it reads ``dx``, ``total_grid_x`` ...)."""
+        if nid in self._cfg:
+            return self._cfg[nid]
+        nd = self.g[nid]
+        inst = nd.inst
+        if inst[0] == "imm":
+            r = nd.name in self.param_names
+        elif inst[0] == "uniop":
+            r = self.om_config_dependent(inst[2])
+        elif inst[0] == "binop":
+            r = self.om_config_dependent(inst[2]) or self.om_config_dependent(inst[3])
+        elif inst[0] == "triop":
+            r = any(self.om_config_dependent(x) for x in inst[2:5])
+        elif inst[0] == "shift":
+            r = self.om_config_dependent(inst[2])
+        else:
+            r = False
+        self._cfg[nid] = r
+        return r
+
+    def om_value(self, nid: int, params: Optional[Dict[str, float]] = None):
+        """Host value of a uniform OM node (each operation rounded once)."""
+        nd = self.g[nid]
+        inst = nd.inst
+        if inst[0] == "imm":
+            if params and nd.name in params:
+                return float(params[nd.name])
+            return float(inst[1])
+        if inst[0] == "shift":
+            return self.om_value(inst[2], params)
+        if inst[0] == "uniop":
+            return fold(inst[:2] + (None,), [self.om_value(inst[2], params)])
+        if inst[0] == "binop":
+            return fold(inst[:2] + (None, None), [self.om_value(inst[2], params),
+                                                   self.om_value(inst[3], params)])
+        if inst[0] == "triop":
+            return fold(inst, [self.om_value(x, params) for x in inst[2:5]])
+        raise FormuraCompileError("not a uniform node")
+
+
+def build_stages(step: List[MMNode]) -> List[Stage]:
+    """Group manifest nodes: reading a node at cursor 0 keeps it in the same
+    stage; reading it at a nonzero cursor needs it in an earlier stage."""
+    stage_of: Dict[int, int] = {}
+    for node in step:
+        st = 0
+        for mn in node.micro:
+            if mn.inst[0] == "loadcursor":
+                dep = mn.inst[2]
+                c = mn.inst[1]
+                need = stage_of[dep] + (0 if all(x == 0 for x in c) else 1)
+                st = max(st, need)
+        stage_of[node.omid] = st
+    # stores go last: they overwrite the state that earlier stages read
+    last = max(stage_of.values())
+    for node in step:
+        if node.is_store:
+            stage_of[node.omid] = last
+    nst = last + 1
+    stages = [Stage(i, [n for n in step if stage_of[n.omid] == i],
+                    any(n.is_store and stage_of[n.omid] == i for n in step)) for i in range(nst)]
+    # which manifest values must go through HBM
+    for node in step:
+        for mn in node.micro:
+            if mn.inst[0] == "loadcursor":
+                dep = mn.inst[2]
+                if stage_of[dep] != stage_of[node.omid]:
+                    s = stages[stage_of[dep]]
+                    if dep not in s.mid_out:
+                        s.mid_out.append(dep)
+    for s in stages:
+        s.mid_out.sort()
+    return stages
+
+
+# --------------------------------------------------------------------------
+# emission
+# --------------------------------------------------------------------------
+_EXT = {"sqrt": "sqrt", "fabs": "fabs", "exp": "exp", "log": "log", "sin": "sin", "cos": "cos"}
+_CMP = {"<", ">", "<=", ">=", "==", "!="}
+
+
+class _StageEmitter:
+    def __init__(self, prog: "_ProgramEmitter", stage: Stage):
+        self.p = prog
+        self.stage = stage
+        self.lines: List[str] = []
+        self.var: Dict[tuple, object] = {}     # key -> expression handle
+        self.n = 0
+
+    def fresh(self) -> str:
+        self.n += 1
+        return f"t{self.n}"
+
+    def emit(self, text: str):
+        self.lines.append("    " + text)
+
+    # expression handles: ('v', name, ctype) or ('lit', float) or ('u', index)
+    # or ('scaled', literal, handle) for an exact product by a power of two
+    def as_T(self, h) -> str:
+        if h[0] == "v":
+            return h[1]
+        if h[0] == "lit":
+            return f"T({c_double(h[1])})"
+        if h[0] == "u":
+            return f"U[{self.p.table_index(h[1])}]"
+        if h[0] == "scaled":
+            return self.materialize(h)
+        raise AssertionError(h)
+
+    def materialize(self, h) -> str:
+        cache = self.p.scaled_cache.setdefault(id(self), {})
+        key = (h[1], self.as_T(h[2]))
+        if key not in cache:
+            name = self.fresh()
+            self.emit(f"const T {name} = M::mul(T({c_double(h[1])}), {key[1]});")
+            cache[key] = name
+        return cache[key]
+
+    def uniform_handle(self, omid: int):
+        an = self.p.an
+        if an.om_config_dependent(omid):
+            return ("u", ("node", omid))
+        v = an.om_value(omid)
+        if isinstance(v, bool):
+            return ("lit", 1.0 if v else 0.0)
+        return ("lit", v)
+
+    def recip_handle(self, omid: int):
+        an = self.p.an
+        if an.om_config_dependent(omid):
+            return ("u", ("recip", omid))
+        return ("lit", 1.0 / an.om_value(omid))
+
+    def node(self, node: MMNode):
+        micro = node.micro
+        for idx, mn in enumerate(micro):
+            key = mn.key
+            if key in self.var:
+                continue
+            h = self.micro(mn, micro, node)
+            if h is not None:
+                self.var[key] = h
+        if node.omid in self.stage.mid_out:
+            root = self.var[micro[-1].key]
+            k = self.p.mids.index(node.omid)
+            self.emit(f"a.template stm<{k}>({self.as_T(root)});")
+
+    def operand(self, micro, i):
+        return self.var[micro[i].key]
+
+    def micro(self, mn: MicroNode, micro, node: MMNode):
+        inst = mn.inst
+        k = inst[0]
+        an = self.p.an
+        omid = mn.key[1]
+        if k in ("imm", "uniop", "binop", "triop") and an.om_uniform(omid):
+            return self.uniform_handle(omid)
+        if k == "loadstatic":
+            c = self.p.cursor3(inst[1])
+            f = self.p.fields.index(inst[2])
+            name = self.fresh()
+            self.emit(f"const T {name} = a.template ld<{f}, {c[0]}, {c[1]}, {c[2]}>();")
+            return ("v", name, "T")
+        if k == "loadcursor":
+            dep = inst[2]
+            c = self.p.cursor3(inst[1])
+            kk = self.p.mids.index(dep)
+            name = self.fresh()
+            self.emit(f"const T {name} = a.template ldm<{kk}, {c[0]}, {c[1]}, {c[2]}>();")
+            return ("v", name, "T")
+        if k == "loadindex":
+            raise FormuraCompileError("index variables inside the step function are not supported "
+                                      "by the GPU backend")
+        if k == "store":
+            f = self.p.fields.index(inst[1])
+            self.emit(f"a.template st<{f}>({self.as_T(self.operand(micro, inst[2]))});")
+            return None
+        if k == "uniop":
+            x = self.operand(micro, inst[2])
+            op = inst[1]
+            if op == "+":
+                return x
+            if op == "-":
+                return self.bind(f"M::neg({self.as_T(x)})")
+            f = op[len("external-call/"):]
+            if f not in _EXT:
+                raise FormuraCompileError(f"external function {f} is not available on the GPU")
+            return self.bind(f"M::{_EXT[f]}({self.as_T(x)})")
+        if k == "binop":
+            op = inst[1]
+            a = self.operand(micro, inst[2])
+            b = self.operand(micro, inst[3])
+            if op in _CMP:
+                return self.bind(f"({self.as_T(a)} {op} {self.as_T(b)})", "bool")
+            if op in ("&&", "||"):
+                return self.bind(f"({self.as_bool(a)} {op} {self.as_bool(b)})", "bool")
+            if op == "*":
+                for x, y in ((a, b), (b, a)):
+                    if x[0] == "lit":
+                        if x[1] == 1.0:
+                            return y
+                        if x[1] == -1.0:
+                            return self.bind(f"M::neg({self.as_T(y)})")
+                        if is_pow2(x[1]) and y[0] != "scaled":
+                            return ("scaled", x[1], y)
+                return self.bind(f"M::mul({self.as_T(a)}, {self.as_T(b)})")
+            if op in ("+", "-"):
+                if b[0] == "scaled":
+                    c = b[1] if op == "+" else -b[1]
+                    return self.bind(f"M::fma(T({c_double(c)}), {self.as_T(b[2])}, {self.as_T(a)})")
+                if a[0] == "scaled":
+                    rhs = self.as_T(b) if op == "+" else f"M::neg({self.as_T(b)})"
+                    return self.bind(f"M::fma(T({c_double(a[1])}), {self.as_T(a[2])}, {rhs})")
+                fn = "add" if op == "+" else "sub"
+                return self.bind(f"M::{fn}({self.as_T(a)}, {self.as_T(b)})")
+            if op == "/":
+                dep = micro[inst[3]].key[1]
+                if an.om_uniform(dep):
+                    if b[0] == "lit" and is_pow2(b[1]):
+                        return self.bind(f"M::mul({self.as_T(a)}, T({c_double(1.0 / b[1])}))")
+                    rc = self.recip_handle(dep)
+                    return self.bind(f"M::divu({self.as_T(a)}, {self.as_T(b)}, {self.as_T(rc)})")
+                return self.bind(f"M::div({self.as_T(a)}, {self.as_T(b)})")
+            if op == "**":
+                if b[0] == "lit" and b[1] == 2.0:
+                    xa = self.as_T(a)
+                    return self.bind(f"M::mul({xa}, {xa})")
+                return self.bind(f"M::pow({self.as_T(a)}, {self.as_T(b)})")
+            raise FormuraCompileError(f"operator {op} is not supported by the GPU backend")
+        if k == "triop":
+            c = self.operand(micro, inst[2])
+            x = self.operand(micro, inst[3])
+            y = self.operand(micro, inst[4])
+            return self.bind(f"({self.as_bool(c)} ? {self.as_T(x)} : {self.as_T(y)})")
+        raise FormuraCompileError(f"cannot emit {k}")
+
+    def as_bool(self, h) -> str:
+        if h[0] == "v" and h[2] == "bool":
+            return h[1]
+        if h[0] == "lit":
+            return "true" if h[1] != 0.0 else "false"
+        return f"({self.as_T(h)} != T(0))"
+
+    def bind(self, expr: str, ctype: str = "T"):
+        name = self.fresh()
+        self.emit(f"const {ctype} {name} = {expr};")
+        return ("v", name, ctype)
+
+
+class _ProgramEmitter:
+    def __init__(self, mm: MMProgram, name: str, runtime_params: List[str]):
+        self.mm = mm
+        self.name = name
+        self.dim = mm.om.genv.dimension
+        if self.dim > 3:
+            raise FormuraCompileError("the GPU backend supports 1, 2 and 3 dimensions")
+        self.fields = mm.fields
+        self.an = _Analysis(mm, runtime_params)
+        self.runtime_params = list(runtime_params)
+        self.stages = build_stages(mm.step)
+        self.mids = sorted({m for s in self.stages for m in s.mid_out})
+        self.table: List[tuple] = []
+        self.scaled_cache: Dict[int, dict] = {}
+        rng = calc_range(mm.step)
+        s = mm.om.config.sleeve
+        stores = [n for n in mm.step if n.is_store]
+        offs = {rng[n.omid].offset() for n in stores}
+        sizes = {rng[n.omid].size() for n in stores}
+        if len(offs) != 1 or sizes != {2 * s}:
+            raise FormuraCompileError(
+                "the stores of this program cover a different extent than the sleeve; the "
+                "reference's loop nest would write outside the grid")
+        self.shift = 2 * s - offs.pop()
+        reach = 0
+        for n in mm.step:
+            for mn in n.micro:
+                if mn.inst[0] in ("loadstatic", "loadcursor"):
+                    reach = max(reach, max(abs(x) for x in mn.inst[1]))
+        self.reach = reach
+
+    def cursor3(self, c) -> List[int]:
+        c = list(c)
+        return [0] * (3 - len(c)) + c
+
+    def table_index(self, entry) -> int:
+        if entry not in self.table:
+            self.table.append(entry)
+        return self.table.index(entry)
+
+    def emit(self) -> KernelProgram:
+        out = [f"// Device code generated by formura_gb300.generator.cuda for program '{self.name}'.",
+               f"// Stencil expressions come from the program's step function; the kernel",
+               f"// templates live in fgb_templates.cuh.",
+               '#include "fgb_templates.cuh"', "",
+               f"namespace fgb_gen_{self.name} {{", ""]
+        stage_texts = []
+        for st in self.stages:
+            se = _StageEmitter(self, st)
+            for node in st.nodes:
+                se.node(node)
+            body = "\n".join(se.lines)
+            stage_texts.append(
+                f"struct Stage{st.index} {{\n"
+                f"  static constexpr bool kWritesState = {'true' if st.writes_state else 'false'};\n"
+                f"  static constexpr int kMidOut = {len(st.mid_out)};\n"
+                f"  template <class M, class A>\n"
+                f"  static __device__ __forceinline__ void run(const A& a, const typename M::T* __restrict__ U) {{\n"
+                f"    using T = typename M::T;\n"
+                f"    (void)U;\n{body}\n  }}\n}};\n")
+        out.append(f"struct Prog {{\n"
+                   f"  static constexpr int kDim = {self.dim};\n"
+                   f"  static constexpr int kFields = {len(self.fields)};\n"
+                   f"  static constexpr int kMids = {len(self.mids)};\n"
+                   f"  static constexpr int kStages = {len(self.stages)};\n"
+                   f"  static constexpr int kSleeve = {self.mm.om.config.sleeve};\n"
+                   f"  static constexpr int kShift = {self.shift};\n"
+                   f"  static constexpr int kReach = {self.reach};\n"
+                   f"  static constexpr int kUniforms = {len(self.table)};\n"
+                   f"}};\n")
+        out += stage_texts
+        out.append(f"}}  // namespace fgb_gen_{self.name}\n")
+        stage_list = ", ".join(f"fgb_gen_{self.name}::Stage{i}" for i in range(len(self.stages)))
+        names = ", ".join(f'"{f}"' for f in self.fields)
+        out.append(f"static const char* const fgb_fields_{self.name}[] = {{{names}}};")
+        out.append(f"FGB_DEFINE_PROGRAM({self.name}, fgb_gen_{self.name}::Prog, fgb_fields_{self.name}, {stage_list})")
+        return KernelProgram(self.name, self.dim, list(self.mm.om.genv.axes), list(self.fields),
+                             self.mm.om.config.sleeve, self.shift, self.reach, self.stages,
+                             self.mids, list(self.table), self.runtime_params, "\n".join(out) + "\n")
+
+
+def emit_cuda(mm: MMProgram, name: str, runtime_params: Optional[List[str]] = None) -> KernelProgram:
+    return _ProgramEmitter(mm, name, runtime_params or []).emit()
+
+
+def uniform_table(mm: MMProgram, kp: KernelProgram, params: Optional[Dict[str, float]] = None) -> List[float]:
+    """Host values of the runtime uniform table for one configuration."""
+    an = _Analysis(mm, kp.runtime_params)
+    out = []
+    for kind, omid in kp.uniform_exprs:
+        v = an.om_value(omid, params)
+        out.append(float(v) if kind == "node" else 1.0 / float(v))
+    return out

@@ -26,6 +26,7 @@ from .translate import FormuraCompileError, Graph, OMProgram, elem_of
 class MicroNode:
     inst: tuple
     type: str          # element type name
+    key: tuple = ()    # (cursor, OM node id) this micro node evaluates
 
 
 @dataclass
@@ -59,7 +60,7 @@ class _Manifester:
         if j is None:
             j = len(self.map)
             self.map[key] = j
-        self.mm[j] = MicroNode(inst, elem_of(self.g[i].type))
+        self.mm[j] = MicroNode(inst, elem_of(self.g[i].type), key)
         return j
 
     def code_at(self, c, nid):

@@ -1,0 +1,94 @@
+/* formura_gb300: C ABI of the GB300 backend for Formura-generated stencil code.
+ *
+ * The reference's boundary is the C pair that Formura writes for each program
+ * (src/Formura/Generator/Encode.hs:11-27): the header declares
+ * `Formura_Grid_Struct formura_data`, `Formura_Navi`, `to_pos_*`,
+ * `Formura_Init`, `Formura_Forward` and `Formura_Finalize`
+ * (src/Formura/Generator/Templates.hs:53-115, 221-250, 295-334, 383-386).
+ * That API stays unchanged: the generator of this backend writes the same
+ * header and a C body whose Formura_Forward calls the entry points below
+ * instead of running the OpenMP loop nests.  Every entry point returns 0 on
+ * success or a negative FGB_E* code; fgb_last_error() describes the last
+ * failure of the calling thread.  No entry point exits the process (the
+ * reference's only error path is exit(1) on an MPI size mismatch,
+ * Templates.hs:243).
+ */
+#ifndef FORMURA_GB300_H
+#define FORMURA_GB300_H
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define FGB_OK 0
+#define FGB_E_ARG (-1)       /* invalid argument */
+#define FGB_E_PROGRAM (-2)   /* unknown program name */
+#define FGB_E_CUDA (-3)      /* CUDA runtime error */
+#define FGB_E_NOMEM (-4)     /* device allocation failed */
+#define FGB_E_NODEV (-5)     /* no CUDA device */
+
+/* Arithmetic forms of the state update. */
+#define FGB_F64 0       /* FP64, rounded like the reference's C (bit-faithful) */
+#define FGB_F64_FAST 1  /* FP64 with fused multiply-add and reciprocal products */
+#define FGB_F32 2       /* FP32 storage and arithmetic */
+#define FGB_F16 3       /* FP16 storage with a per-field scale, FP32 arithmetic */
+
+typedef struct fgb_grid fgb_grid;
+
+/* Programs compiled into the library.  A program is the step function of a
+ * .fmr file; its kernels are the hand-written templates instantiated with
+ * the program's stencil expression. */
+int fgb_program_count(void);
+const char* fgb_program_name(int index);
+/* dim, number of state fields, size of the uniform table, sleeve
+ * (calcSleeve, src/Formura/OrthotopeMachine/Translate.hs:613-623) and the
+ * per-step roll of the array content (Templates.hs:346). */
+int fgb_program_query(const char* program, int* dim, int* nfields, int* nuniforms,
+                      int* sleeve, int* shift);
+/* Name of state field `index` (fields are in name order, like the members of
+ * Formura_Grid_Struct, Templates.hs:53-73). */
+const char* fgb_program_field(const char* program, int index);
+
+/* Create a device-resident grid of `program` with extent shape[0..ndim-1]
+ * (the grid_per_node of the numerical config) in the given precision.
+ * `uniforms` holds the grid-independent values of the step function for
+ * this configuration, in the order the generator reports. Replaces the
+ * static buffers of Templates.hs:125-186. */
+int fgb_open(const char* program, const int* shape, int ndim, int precision,
+             const double* uniforms, int nuniforms, fgb_grid** out);
+int fgb_close(fgb_grid* grid);
+
+/* FP16 storage: value = stored * scales[f]. */
+int fgb_set_scales(fgb_grid* grid, const float* scales, int nfields);
+
+/* Copy the whole state between the host and the device.  `host_state`
+ * points at a Formura_Grid_Struct: one C-order array per field, fields back
+ * to back in name order, FP64 (the layout of formura_data). */
+int fgb_upload(fgb_grid* grid, const double* host_state);
+int fgb_download(fgb_grid* grid, double* host_state);
+
+/* Advance `nsteps` time steps (enqueued on the grid's stream).  Each step
+ * rolls the array content by the program's shift along every axis, exactly
+ * as Formura_Forward does (Templates.hs:300-310, 336-346). */
+int fgb_forward(fgb_grid* grid, int nsteps);
+int fgb_synchronize(fgb_grid* grid);
+
+/* The grid's CUDA stream (a cudaStream_t), for events and interop. */
+void* fgb_stream(fgb_grid* grid);
+/* Device pointers of the current state fields (storage precision). */
+int fgb_state_device(fgb_grid* grid, void** field_ptrs, int nfields);
+/* Number of kernels this grid has launched so far. */
+int64_t fgb_launch_count(fgb_grid* grid);
+
+/* Pin a host range (e.g. formura_data) for faster copies; optional. */
+int fgb_host_register(void* ptr, size_t bytes);
+int fgb_host_unregister(void* ptr);
+
+const char* fgb_last_error(void);
+
+#ifdef __cplusplus
+}
+#endif
+#endif

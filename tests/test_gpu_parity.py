@@ -1,0 +1,129 @@
+"""Parity of the GB300 drop-in against the oracle, through the generated C API.
+
+Both sides are driven exactly like a Formura driver program: Formura_Init,
+the seeded state written into formura_data, Formura_Forward called in a loop,
+formura_data and Formura_Navi read back.  The FP64 form must match the
+oracle bit for bit (rel-L2 0, well inside the 1e-12 bound); integer grid
+indexing (offset_*, time_step) must be identical.
+"""
+import numpy as np
+import pytest
+
+from formura_gb300 import workloads as W
+from formura_gb300.host import FormuraProgram, builtin_program
+from oracle.reference_lib import ReferenceProgram
+
+pytestmark = pytest.mark.gpu
+
+
+def _pair(program, cfg_text, gpu_extra="", tag="t"):
+    src, _ = builtin_program(program)
+    ref = ReferenceProgram(src, cfg_text, f"{program}_{tag}_ref")
+    gpu = FormuraProgram(src, cfg_text + gpu_extra, program, name=f"{program}_{tag}_gpu")
+    return ref, gpu
+
+
+def _check_navi(a, b):
+    assert a == b, (a, b)
+
+
+@pytest.mark.parametrize("n,steps,spf", [(16, 9, 1), (32, 40, 8), (20, 33, 11)])
+def test_heat_f64_bit_exact(n, steps, spf):
+    cfg = W.heat_config(n)
+    ref, gpu = _pair("heat3d", cfg, f"gpu_steps_per_forward: {spf}\n", f"n{n}s{spf}")
+    _check_navi(ref.init(), gpu.init())
+    x = W.heat_state((n, n, n), seed=n)["q"]
+    ref.set("q", x)
+    gpu.set("q", x)
+    calls = steps // spf
+    for _ in range(calls):
+        ref.forward(spf)
+        gpu.forward(1)
+    _check_navi(ref.navi_dict(), gpu.navi_dict())
+    a, b = ref.get("q"), gpu.get("q")
+    assert np.array_equal(a, b), f"max |diff| {np.abs(a - b).max()}"
+    gpu.finalize()
+
+
+def test_heat_full_config_bit_exact():
+    """128^3, D*dt/dx^2 = 0.1, 1000 steps, uniform [0,1) from a seed."""
+    n, steps = 128, 1000
+    cfg = W.heat_config(n)
+    ref, gpu = _pair("heat3d", cfg, "gpu_steps_per_forward: 1000\n", "full")
+    ref.init()
+    gpu.init()
+    x = W.heat_state((n, n, n), seed=0)["q"]
+    ref.set("q", x)
+    gpu.set("q", x)
+    ref.forward(steps)
+    gpu.forward(1)
+    _check_navi(ref.navi_dict(), gpu.navi_dict())
+    a, b = ref.get("q"), gpu.get("q")
+    assert np.array_equal(a, b), f"rel-L2 {W.rel_l2(b, a)}"
+    # the periodic explicit scheme conserves the total up to rounding
+    assert abs(b.sum() - x.sum()) < 1e-9 * x.size
+    gpu.finalize()
+
+
+@pytest.mark.parametrize("n,steps,spf", [(64, 50, 1), (96, 300, 50)])
+def test_gray_scott_f64_bit_exact(n, steps, spf):
+    cfg = W.gs_config(n)
+    ref, gpu = _pair("gs2d", cfg, f"gpu_steps_per_forward: {spf}\n", f"n{n}s{spf}")
+    _check_navi(ref.init(), gpu.init())
+    for f in ("u", "v"):
+        assert np.array_equal(ref.get(f), gpu.get(f)), "init differs"
+    st = W.gs_perturb(ref.get("u"), ref.get("v"), seed=7)
+    for f in ("u", "v"):
+        ref.set(f, st[f])
+        gpu.set(f, st[f])
+    for _ in range(steps // spf):
+        ref.forward(spf)
+        gpu.forward(1)
+    _check_navi(ref.navi_dict(), gpu.navi_dict())
+    for f in ("u", "v"):
+        a, b = ref.get(f), gpu.get(f)
+        assert np.array_equal(a, b), f"{f}: max |diff| {np.abs(a - b).max()}"
+    gpu.finalize()
+
+
+def test_gray_scott_4096_bit_exact_200_steps():
+    n, steps = 4096, 200
+    cfg = W.gs_config(n)
+    ref, gpu = _pair("gs2d", cfg, f"gpu_steps_per_forward: {steps}\n", "big")
+    ref.init()
+    gpu.init()
+    st = W.gs_perturb(ref.get("u"), ref.get("v"), seed=0)
+    for f in ("u", "v"):
+        ref.set(f, st[f])
+        gpu.set(f, st[f])
+    ref.forward(steps)
+    gpu.forward(1)
+    _check_navi(ref.navi_dict(), gpu.navi_dict())
+    for f in ("u", "v"):
+        assert np.array_equal(ref.get(f), gpu.get(f))
+    gpu.finalize()
+
+
+@pytest.mark.parametrize("prec,tol", [("f64fast", 1e-12), ("f32", 1e-5), ("f16", 5e-2)])
+def test_gray_scott_reduced_precision(prec, tol):
+    """FP32 / FP16 storage and FP64 with contraction: relative L2 against the
+    FP64 oracle after 500 steps at 128^2 (tolerance stated per form)."""
+    n, steps = 128, 500
+    cfg = W.gs_config(n)
+    extra = f"gpu_precision: {prec}\ngpu_steps_per_forward: {steps}\n"
+    if prec == "f16":
+        extra += "gpu_field_scales: [1.0, 0.5]\n"
+    ref, gpu = _pair("gs2d", cfg, extra, prec)
+    ref.init()
+    gpu.init()
+    st = W.gs_perturb(ref.get("u"), ref.get("v"), seed=3)
+    for f in ("u", "v"):
+        ref.set(f, st[f])
+        gpu.set(f, st[f])
+    ref.forward(steps)
+    gpu.forward(1)
+    _check_navi(ref.navi_dict(), gpu.navi_dict())
+    for f in ("u", "v"):
+        err = W.rel_l2(gpu.get(f), ref.get(f))
+        assert err < tol, f"{prec} {f}: rel-L2 {err}"
+    gpu.finalize()

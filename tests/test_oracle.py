@@ -1,0 +1,159 @@
+"""The oracle (the reference generator's C, restated) checked on the CPU.
+
+Pins, in the absence of numeric golden vectors in the reference (its tests
+cover config decoding only, test/NumericalConfigSpec.hs):
+* temporal blocking and no blocking give identical states (two independent
+  code paths of Templates.hs: 300-310 versus 311-381);
+* the generated loop nests equal independent numpy restatements of the
+  stencils bit for bit, including the per-step roll of the array content;
+* committed golden fixtures (tests/golden, made by make_golden.py) are
+  reproduced, so the oracle is the same on every machine;
+* the reference's own example programs compile and behave the same way
+  (when the reference tree is available).
+"""
+import os
+
+import numpy as np
+import pytest
+
+from formura_gb300 import workloads as W
+from formura_gb300.host import builtin_program
+from oracle.reference_lib import ReferenceProgram
+
+REF = "/root/reference"
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+
+
+def heat_numpy(q, steps, dx):
+    """Independent restatement of heat3d.fmr's update, same operation order."""
+    dt = (0.1 * dx) * dx
+    for _ in range(steps):
+        def second(ax):
+            return ((np.roll(q, -1, ax) - 2.0 * q) + np.roll(q, 1, ax)) / (dx * dx)
+        q = q + dt * ((second(0) + second(1)) + second(2))
+        q = np.roll(q, (1, 1, 1), (0, 1, 2))
+    return q
+
+
+def gs_numpy(u, v, steps, dx):
+    Du, Dv, F, k = 2.0e-5, 1.0e-5, 0.04, 0.06
+    c = dx * dx
+    for _ in range(steps):
+        def lap(a):
+            return ((np.roll(a, -1, 0) - 2.0 * a) + np.roll(a, 1, 0)) / c + \
+                   ((np.roll(a, -1, 1) - 2.0 * a) + np.roll(a, 1, 1)) / c
+        uvv = (u * v) * v
+        un = u + ((Du * lap(u) - uvv) + F * (1.0 - u))
+        vn = v + ((Dv * lap(v) + uvv) - (F + k) * v)
+        u = np.roll(un, (1, 1), (0, 1))
+        v = np.roll(vn, (1, 1), (0, 1))
+    return u, v
+
+
+def test_heat_oracle_equals_numpy_bitwise():
+    n = 12
+    src, _ = builtin_program("heat3d")
+    ref = ReferenceProgram(src, W.heat_config(n), "heat_np")
+    ref.init()
+    x = W.heat_state((n, n, n), 5)["q"]
+    ref.set("q", x)
+    nav = ref.forward(7)
+    assert nav["time_step"] == 7 and nav["offset_x"] == n - 7
+    assert np.array_equal(ref.get("q"), heat_numpy(x, 7, 1.0 / n))
+
+
+def test_gs_oracle_equals_numpy_bitwise():
+    n = 32
+    src, _ = builtin_program("gs2d")
+    ref = ReferenceProgram(src, W.gs_config(n), "gs_np")
+    ref.init()
+    u0, v0 = ref.get("u"), ref.get("v")
+    inside = (np.arange(n) > 0.45 * n) & (np.arange(n) < 0.55 * n)
+    sq = inside[:, None] & inside[None, :]
+    assert np.array_equal(u0, np.where(sq, 0.5, 1.0)) and np.array_equal(v0, np.where(sq, 0.25, 0.0))
+    st = W.gs_perturb(u0, v0, 4)
+    ref.set("u", st["u"])
+    ref.set("v", st["v"])
+    ref.forward(20)
+    u, v = gs_numpy(st["u"], st["v"], 20, 0.01)
+    assert np.array_equal(ref.get("u"), u) and np.array_equal(ref.get("v"), v)
+
+
+def test_temporal_blocking_equals_no_blocking():
+    src, _ = builtin_program("heat3d")
+    n = 12
+    nb = ReferenceProgram(src, W.heat_config(n), "heat_nb")
+    tb = ReferenceProgram(src, W.heat_config(n, extra="grid_per_block: [4, 4, 4]\n"
+                                                     "temporal_blocking_interval: 2\n"), "heat_tb")
+    nb.init()
+    tb.init()
+    x = W.heat_state((n, n, n), 1)["q"]
+    nb.set("q", x)
+    tb.set("q", x)
+    nb.forward(6)
+    tb.forward(3)
+    assert nb.navi_dict() == tb.navi_dict()
+    assert np.array_equal(nb.get("q"), tb.get("q"))
+
+
+@pytest.mark.parametrize("name", ["heat3d_16_10", "gs2d_64_50"])
+def test_golden_fixture_reproduced(name):
+    path = os.path.join(GOLDEN, name + ".npz")
+    d = np.load(path)
+    prog = str(d["program"])
+    src, _ = builtin_program(prog)
+    ref = ReferenceProgram(src, str(d["config"]), f"golden_{name}")
+    ref.init()
+    for f in ref.fields:
+        ref.set(f, d["in_" + f])
+    ref.forward(int(d["steps"]))
+    for f in ref.fields:
+        assert np.array_equal(ref.get(f), d["out_" + f]), f
+    assert ref.navi_dict()["offset_x"] == int(d["offset_x"])
+
+
+def _ref_file(*p):
+    path = os.path.join(REF, *p)
+    if not os.path.exists(path):
+        pytest.skip("reference tree not available")
+    return open(path).read()
+
+
+def test_reference_diffusion3_blocking_paths_agree():
+    src = _ref_file("examples", "diffusion3", "diffusion3.fmr")
+    tb_cfg = _ref_file("examples", "diffusion3", "diffusion3.yaml")
+    tb = ReferenceProgram(src, tb_cfg, "ref_d3_tb")
+    nb = ReferenceProgram(src, "length_per_node: [1.0,1.0,1.0]\ngrid_per_node: [100,100,100]\n", "ref_d3_nb")
+    for p in (tb, nb):
+        p.init()
+    assert np.array_equal(tb.get("q"), nb.get("q"))
+    x = W.heat_state((100, 100, 100), 3)["q"]
+    tb.set("q", x)
+    nb.set("q", x)
+    tb.forward(2)
+    nb.forward(10)
+    assert tb.navi_dict() == nb.navi_dict()
+    assert np.array_equal(tb.get("q"), nb.get("q"))
+    # examples/diffusion3/diffusion3.fmr: (q[i+1] + q[i-1] - 2*q[i])/dx**2
+    q, dx = x, 0.01
+    dt = (0.1 * dx) * dx
+    for _ in range(10):
+        def d2(ax):
+            return ((np.roll(q, -1, ax) + np.roll(q, 1, ax)) - 2.0 * q) / dx ** 2
+        q = np.roll(q + dt * ((d2(0) + d2(1)) + d2(2)), (1, 1, 1), (0, 1, 2))
+    assert np.array_equal(nb.get("q"), q)
+
+
+def test_reference_samples_compile():
+    from formura_gb300.generator.config import decode_config
+    from formura_gb300.generator.manifest import compile_program
+    cases = {("sample", "3d_hllc", "3d_hllc.fmr", "config.yaml"): (2, 64, ["e", "rho", "rhou", "rhov", "rhow"]),
+             ("sample", "1d_hllc", "hllc.fmr", "config.yaml"): (2, 28, ["e", "rho", "rhou", "rhov", "rhow"]),
+             ("sample", "mhd_3d_hlld", "mhd_3d_hlld.fmr", "config.yaml"): (2, 108, None),
+             ("examples", "pearson2", "pearson2.fmr", "pearson2.yaml"): (1, 2, ["u", "v"])}
+    for (a, b, f, y), (sleeve, nman, fields) in cases.items():
+        mm = compile_program(_ref_file(a, b, f), decode_config(_ref_file(a, b, y)))
+        assert mm.om.config.sleeve == sleeve
+        assert len(mm.step) == nman
+        if fields:
+            assert mm.fields == fields
