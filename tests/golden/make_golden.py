@@ -1,7 +1,15 @@
-"""Writes the golden fixtures of tests/golden: the oracle's output (the
-reference generator's C, restated, compiled with gcc) for small seeded runs
-of the shipped programs.  Run from the repository root:
-    python tests/golden/make_golden.py
+"""Writes the golden fixtures of tests/golden from the reference's own
+programs, run through the restated Formura generator (the oracle):
+
+* examples/diffusion3/diffusion3.fmr on a 16^3 grid (heat workload);
+* examples/pearson2/pearson2.fmr with the Gray-Scott workload's feed rate
+  f = 0.04 (the other parameters already match) on 64^2;
+* sample/3d_hllc/3d_hllc.fmr with Courant number 0.4 on 16^3.
+
+Each fixture stores the seeded input state, the config, the step count and
+the output state and grid offset.  The shipped programs (heat3d, gs2d,
+hllc3d) must reproduce them bit for bit.  Needs the reference tree; run from
+the repository root:  python tests/golden/make_golden.py
 """
 import os
 import sys
@@ -12,28 +20,44 @@ ROOT = os.path.dirname(os.path.dirname(os.path.dirname(os.path.abspath(__file__)
 sys.path.insert(0, ROOT)
 
 from formura_gb300 import workloads as W  # noqa: E402
-from formura_gb300.host import builtin_program  # noqa: E402
 from oracle.reference_lib import ReferenceProgram  # noqa: E402
 
+REF = "/root/reference"
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 
-def make(name, program, cfg, steps, state_fn):
-    src, _ = builtin_program(program)
+def reference_source(path, edits=()):
+    with open(os.path.join(REF, path)) as f:
+        src = f.read()
+    for old, new in edits:
+        assert old in src, old
+        src = src.replace(old, new)
+    return src
+
+
+def make(name, src, cfg, steps, state_fn, field_map):
     ref = ReferenceProgram(src, cfg, f"mkgold_{name}")
     ref.init()
     st = state_fn(ref)
-    for f in ref.fields:
-        ref.set(f, st[f])
+    for mine, theirs in field_map.items():
+        ref.set(theirs, st[mine])
     nav = ref.forward(steps)
-    d = {"program": program, "config": cfg, "steps": steps, "offset_x": nav["offset_x"]}
-    for f in ref.fields:
-        d["in_" + f] = st[f]
-        d["out_" + f] = ref.get(f)
+    d = {"config": cfg, "steps": steps, "offset_x": nav["offset_x"], "time_step": nav["time_step"]}
+    for mine, theirs in field_map.items():
+        d["in_" + mine] = st[mine]
+        d["out_" + mine] = ref.get(theirs)
     np.savez_compressed(os.path.join(OUT, name + ".npz"), **d)
     print("wrote", name)
 
 
 if __name__ == "__main__":
-    make("heat3d_16_10", "heat3d", W.heat_config(16), 10, lambda r: W.heat_state((16, 16, 16), 11))
-    make("gs2d_64_50", "gs2d", W.gs_config(64), 50, lambda r: W.gs_perturb(r.get("u"), r.get("v"), 12))
+    make("heat3d_16_10", reference_source("examples/diffusion3/diffusion3.fmr"), W.heat_config(16), 10,
+         lambda r: W.heat_state((16, 16, 16), 11), {"q": "q"})
+    make("gs2d_64_50", reference_source("examples/pearson2/pearson2.fmr",
+                                        [("double :: f = 0.03", "double :: f = 0.04")]),
+         W.gs_config(64), 50,
+         lambda r: W.gs_perturb(np.ones((64, 64)), np.zeros((64, 64)), 12), {"u": "u", "v": "v"})
+    make("hllc3d_16_5", reference_source("sample/3d_hllc/3d_hllc.fmr",
+                                         [("double :: C_cfl = 0.8", "double :: C_cfl = 0.4")]),
+         W.hllc_config(16), 5, lambda r: W.hllc_state((16, 16, 16), 13),
+         {"e": "e", "mx": "rhou", "my": "rhov", "mz": "rhow", "rho": "rho"})

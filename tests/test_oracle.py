@@ -28,9 +28,9 @@ def heat_numpy(q, steps, dx):
     """Independent restatement of heat3d.fmr's update, same operation order."""
     dt = (0.1 * dx) * dx
     for _ in range(steps):
-        def second(ax):
-            return ((np.roll(q, -1, ax) - 2.0 * q) + np.roll(q, 1, ax)) / (dx * dx)
-        q = q + dt * ((second(0) + second(1)) + second(2))
+        def curv(ax):
+            return ((np.roll(q, -1, ax) + np.roll(q, 1, ax)) - 2.0 * q) / dx ** 2
+        q = q + dt * ((curv(0) + curv(1)) + curv(2))
         q = np.roll(q, (1, 1, 1), (0, 1, 2))
     return q
 
@@ -40,11 +40,10 @@ def gs_numpy(u, v, steps, dx):
     c = dx * dx
     for _ in range(steps):
         def lap(a):
-            return ((np.roll(a, -1, 0) - 2.0 * a) + np.roll(a, 1, 0)) / c + \
-                   ((np.roll(a, -1, 1) - 2.0 * a) + np.roll(a, 1, 1)) / c
-        uvv = (u * v) * v
-        un = u + ((Du * lap(u) - uvv) + F * (1.0 - u))
-        vn = v + ((Dv * lap(v) + uvv) - (F + k) * v)
+            return ((np.roll(a, -1, 0) + np.roll(a, 1, 0)) - 2.0 * a) / c + \
+                   ((np.roll(a, -1, 1) + np.roll(a, 1, 1)) - 2.0 * a) / c
+        un = u + ((Du * lap(u) - (u * v) * v) + F * (1.0 - u))
+        vn = v + ((Dv * lap(v) + (u * v) * v) - (F + k) * v)
         u = np.roll(un, (1, 1), (0, 1))
         v = np.roll(vn, (1, 1), (0, 1))
     return u, v
@@ -96,20 +95,21 @@ def test_temporal_blocking_equals_no_blocking():
     assert np.array_equal(nb.get("q"), tb.get("q"))
 
 
-@pytest.mark.parametrize("name", ["heat3d_16_10", "gs2d_64_50"])
-def test_golden_fixture_reproduced(name):
-    path = os.path.join(GOLDEN, name + ".npz")
-    d = np.load(path)
-    prog = str(d["program"])
-    src, _ = builtin_program(prog)
+@pytest.mark.parametrize("name,program", [("heat3d_16_10", "heat3d"), ("gs2d_64_50", "gs2d"),
+                                          ("hllc3d_16_5", "hllc3d")])
+def test_golden_fixture_reproduced(name, program):
+    """The shipped programs reproduce, bit for bit, the reference's own
+    example programs (fixtures made by tests/golden/make_golden.py)."""
+    d = np.load(os.path.join(GOLDEN, name + ".npz"))
+    src, _ = builtin_program(program)
     ref = ReferenceProgram(src, str(d["config"]), f"golden_{name}")
     ref.init()
     for f in ref.fields:
         ref.set(f, d["in_" + f])
-    ref.forward(int(d["steps"]))
+    nav = ref.forward(int(d["steps"]))
     for f in ref.fields:
         assert np.array_equal(ref.get(f), d["out_" + f]), f
-    assert ref.navi_dict()["offset_x"] == int(d["offset_x"])
+    assert nav["offset_x"] == int(d["offset_x"]) and nav["time_step"] == int(d["time_step"])
 
 
 def _ref_file(*p):
