@@ -347,3 +347,6 @@ int fgb_host_unregister(void* ptr) {
 }
 
 }  // extern "C"
+
+// Lets other translation units of the library report through fgb_last_error().
+int fgb_internal_set_error(int code, const char* message) { return fail(code, "%s", message); }

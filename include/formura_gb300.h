@@ -88,6 +88,35 @@ int fgb_host_unregister(void* ptr);
 
 const char* fgb_last_error(void);
 
+/* Size of the fixed device array that fgb_forward_noalloc draws on. */
+#define FGB_NOALLOC_SCRATCH_BYTES (64ull << 20)
+
+/* Advance a caller-owned device state by `nsteps` steps without allocating
+ * any device memory.  This entry point has no counterpart in the reference
+ * (whose generated code keeps every buffer in static host arrays); it serves
+ * callers that cannot call cudaMalloc while they run, such as a framework
+ * that owns all device memory through its own pool, or a plug-in host that
+ * forbids device allocation once a run has started.
+ *
+ * in_state / out_state: device pointers to the whole state in the
+ * formura_data layout (fields back to back, name order), in the storage
+ * type of `precision` (FGB_F16 uses unit scales).  They must not overlap;
+ * in_state is left unchanged.  The uniform table, the second buffer of the
+ * step-to-step ping-pong and the intermediate arrays of multi-stage programs
+ * come from one static device array of FGB_NOALLOC_SCRATCH_BYTES (64 MiB),
+ * which every GPU that loads the library holds until the process exits.  A
+ * grid that needs more returns FGB_E_ARG with the required size.  Nothing in
+ * that array has to start at zero: every byte a call reads was written
+ * earlier by the same call.  All calls share the array, so calls that
+ * overlap on the GPU (other streams, other host threads) race and must be
+ * serialised by the caller.  The first call on each device looks up the
+ * array's device address; make that first call before any stream capture.
+ * Work is queued on `stream` (a cudaStream_t; NULL is the legacy default
+ * stream) and is complete when that stream is. */
+int fgb_forward_noalloc(const char* program, const int* shape, int ndim, int precision,
+                        const double* uniforms, int nuniforms, const void* in_state,
+                        void* out_state, int nsteps, void* stream);
+
 #ifdef __cplusplus
 }
 #endif
