@@ -103,6 +103,11 @@ def workload_spec(name: str):
         return {"program": "heat3d", "cfg": W.heat_config(n), "shape": (n, n, n), "fields": 1,
                 "steps_total": 1000,
                 "label": "heat-3d 128^3 periodic, D*dt/dx^2=0.1, 1000 steps"}
+    if name == "hllc3d":
+        n = 256
+        return {"program": "hllc3d", "cfg": W.hllc_config(n), "shape": (n, n, n), "fields": 5,
+                "steps_total": 500, "cpu_cfg": W.hllc_config(128), "cpu_shape": (128, 128, 128),
+                "label": "hllc-euler-3d 256^3 periodic, gamma=1.4, MUSCL-minmod + HLLC, CFL 0.4, 500 steps"}
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -113,6 +118,9 @@ def initial_state(spec, prog):
     if spec["program"] == "gs2d":
         st = W.gs_perturb(prog.get("u"), prog.get("v"), seed=0)
         return np.stack([st["u"], st["v"]])
+    if spec["program"] == "hllc3d":
+        st = W.hllc_state(tuple(prog.shape), seed=0)
+        return np.stack([st[f] for f in prog.fields])
     return W.heat_state(spec["shape"], seed=0)["q"][None]
 
 
@@ -125,7 +133,8 @@ def run_reference(args, spec):
     from formura_gb300.host import builtin_program
     from oracle.reference_lib import ReferenceProgram
     src, _ = builtin_program(spec["program"])
-    ref = ReferenceProgram(src, spec["cfg"], f"{spec['program']}_bench_ref")
+    cfg = spec.get("cpu_cfg", spec["cfg"])
+    ref = ReferenceProgram(src, cfg, f"{spec['program']}_bench_ref_{spec.get('cpu_shape', spec['shape'])[0]}")
     ref.init()
     st = initial_state(spec, ref)
     for i, f in enumerate(ref.fields):
@@ -137,7 +146,7 @@ def run_reference(args, spec):
         ref.forward(1)
     dt = time.perf_counter() - t0
     cells = 1
-    for x in spec["shape"]:
+    for x in spec.get("cpu_shape", spec["shape"]):
         cells *= x
     v = cells * args.steps / dt / 1e9
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
@@ -224,6 +233,8 @@ def run_ours(args, spec):
         return g
 
     g = open_grid(args.precision)
+    tuned = g.autotune(32) if not args.no_autotune else -1
+    variant = next((v for v in g.variants() if v["index"] == tuned), None)
     stream = torch.cuda.ExternalStream(g.stream)
     sampler = ClockSampler(local)
     if ws > 1:
@@ -239,15 +250,20 @@ def run_ours(args, spec):
     tsteps = args.steps * spf
     value = ws * cells * tsteps / (ms / 1e3) / 1e9
 
-    # roofline of the dominant (only) kernel: one stage launch per time step
-    per_launch_ms = ms / max(1, launches)
-    bytes_per_launch = 2 * nf * storage_bytes(args.precision) * cells
+    # roofline: algorithmic bytes of one time step (read + write of every state
+    # field) over the time of one step; single-stage programs launch one
+    # kernel per step, so this is the per-launch figure of that kernel
+    stages = max(1, launches // max(1, tsteps))
+    per_step_ms = ms / tsteps
+    bytes_per_step = 2 * nf * storage_bytes(args.precision) * cells
     peak, peak_kind = measured_peaks()
-    achieved = bytes_per_launch / (per_launch_ms / 1e3) / 1e9
+    achieved = bytes_per_step / (per_step_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind,
                 "traffic": load_traffic(spec, args.precision),
-                "algorithmic_bytes_per_launch": bytes_per_launch, "avg_launch_us": per_launch_ms * 1e3}
+                "algorithmic_bytes_per_launch": bytes_per_step if stages == 1 else None,
+                "algorithmic_bytes_per_step": bytes_per_step, "kernels_per_step": stages,
+                "avg_step_us": per_step_ms * 1e3}
 
     # end to end through the drop-in C API: upload + spf steps + download per call
     for _ in range(2):
@@ -266,11 +282,13 @@ def run_ours(args, spec):
     if rank == 0 and not args.no_variants and args.precision == "f64":
         for prec in ("f32", "f16"):
             gv = open_grid(prec)
+            tv = gv.autotune(32) if not args.no_autotune else -1
             sv = torch.cuda.ExternalStream(gv.stream)
             vms, _ = time_grid(gv, spf, args.warmup, args.steps, torch, sv)
             fin = gv.download()
             errs = {f: W.rel_l2(fin[i], final64[i]) for i, f in enumerate(dp.fields)}
-            variants[prec] = {"value": cells * tsteps / (vms / 1e3) / 1e9, "unit": "GLUP/s",
+            variants[prec] = {"kernel": next((v for v in gv.variants() if v["index"] == tv), "one step per launch"),
+                              "value": cells * tsteps / (vms / 1e3) / 1e9, "unit": "GLUP/s",
                               "speedup_vs_f64": (cells * tsteps / (vms / 1e3) / 1e9) / value * ws,
                               "rel_l2_vs_f64_oracle": errs,
                               "time_steps": (args.warmup + args.steps) * spf}
@@ -286,6 +304,7 @@ def run_ours(args, spec):
                 "scaling": "weak", "vs_baseline": None, "dtype": args.precision, "data": "synthetic",
                 "config": {"workload": spec["label"], "time_steps_per_bench_step": spf,
                            "timed_time_steps": tsteps, "precision": args.precision,
+                           "kernel": variant if variant else "one step per launch (generic stage kernel)",
                            "l2": "state (2 buffers x %d MB) larger than the 129 MB L2" %
                                  (nf * cells * storage_bytes(args.precision) // 2**20),
                            "parallelism": "replicas" if ws > 1 else "single GPU"},
@@ -306,7 +325,9 @@ def cpu_baseline(spec, args):
     from formura_gb300.host import builtin_program
     from oracle.reference_lib import ReferenceProgram
     src, _ = builtin_program(spec["program"])
-    ref = ReferenceProgram(src, spec["cfg"], f"{spec['program']}_bench_ref")
+    cfg = spec.get("cpu_cfg", spec["cfg"])
+    shape = spec.get("cpu_shape", spec["shape"])
+    ref = ReferenceProgram(src, cfg, f"{spec['program']}_bench_ref_{shape[0]}")
     ref.init()
     st = initial_state(spec, ref)
     for i, f in enumerate(ref.fields):
@@ -320,11 +341,12 @@ def cpu_baseline(spec, args):
     ref.forward(n)
     dt = time.perf_counter() - t0
     cells = 1
-    for x in spec["shape"]:
+    for x in shape:
         cells *= x
     cores = int(os.environ.get("OMP_NUM_THREADS", os.cpu_count() or 1))
+    grid = "x".join(str(x) for x in shape)
     return {"value": cells * n / dt / 1e9, "unit": "GLUP/s", "cores": cores, "kind": "port",
-            "sample": f"{n} time steps of the full {spec['label'].split(',')[0]} grid ({dt:.1f} s)"}
+            "sample": f"{n} time steps of the {spec['program']} workload on a {grid} grid ({dt:.1f} s)"}
 
 
 def main():
@@ -333,14 +355,27 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="gs2d", choices=["gs2d", "heat3d"])
+    ap.add_argument("--workload", default="gs2d", choices=["gs2d", "heat3d", "hllc3d", "adjoint", "batch"])
     ap.add_argument("--precision", default="f64", choices=["f64", "f64fast", "f32", "f16"])
     ap.add_argument("--spf", type=int, default=100, help="time steps per bench step")
     ap.add_argument("--e2e-steps", type=int, default=20)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--adj-n", type=int, default=512)
+    ap.add_argument("--adj-steps", type=int, default=200)
+    ap.add_argument("--probes", type=int, default=64)
+    ap.add_argument("--time-steps", type=int, default=20)
+    ap.add_argument("--count", type=int, default=256)
+    ap.add_argument("--batch-steps", type=int, default=5000)
     args = ap.parse_args()
+    if args.workload == "adjoint":
+        run_adjoint(args)
+        return
+    if args.workload == "batch":
+        run_batch(args)
+        return
     spec = workload_spec(args.workload)
     if args.steps is None:
         args.steps = max(1, spec["steps_total"] // args.spf) if args.impl == "ours" else 200
@@ -348,6 +383,181 @@ def main():
         run_reference(args, spec)
     else:
         run_ours(args, spec)
+
+
+
+def run_adjoint(args):
+    """Diffusion adjoint and inverse-problem gradient (512^3, D*dt/dx^2 = 0.1,
+    200 steps): dJ/du_0 of J = 0.5*||u_T - u_target||^2 by the generated
+    adjoint with binomial checkpointing (8 snapshots), in FP64 and FP32,
+    checked against central differences (eps 1e-6, FP64) on random probes."""
+    import numpy as np
+    import torch
+    from formura_gb300 import build as B
+    if not os.path.exists(B.LIB):
+        B.build()
+    from formura_gb300 import workloads as W
+    from formura_gb300.host import Grid, builtin_program, program_uniforms
+    n, nsteps, snaps = args.adj_n, args.adj_steps, 8
+    shape = (n, n, n)
+    src, _ = builtin_program("heat3d")
+    _, U = program_uniforms(src, W.heat_config(n), "heat3d")
+
+    def field(seed):
+        rng = np.random.default_rng(seed)
+        dev = "cuda"
+        idx = torch.arange(n, dtype=torch.float64, device=dev)
+        out = torch.zeros(shape, dtype=torch.float64, device=dev)
+        for _ in range(32):
+            c = [rng.uniform(0, n) for _ in range(3)]
+            w = rng.uniform(4.0, 16.0)
+            amp = rng.normal()
+            parts = []
+            for ax in range(3):
+                d = (idx - c[ax]).abs()
+                d = torch.minimum(d, n - d)
+                parts.append(torch.exp(-0.5 * (d / w) ** 2))
+            out += amp * parts[0][:, None, None] * parts[1][None, :, None] * parts[2][None, None, :]
+        return out.cpu().numpy()[None]
+
+    u0, target = field(0), field(1)
+    cells = n ** 3
+    res = {}
+    for prec in ("f64", "f32"):
+        g = Grid("heat3d", shape, prec, U)
+        stream = torch.cuda.ExternalStream(g.stream)
+        g.upload(u0)
+        ev = [torch.cuda.Event(enable_timing=True) for _ in range(4)]
+        g.forward(5)
+        g.synchronize()
+        ev[0].record(stream)
+        g.forward(args.time_steps)
+        ev[1].record(stream)
+        g.adjoint_steps(1)
+        g.synchronize()
+        ev[2].record(stream)
+        g.adjoint_steps(args.time_steps)
+        ev[3].record(stream)
+        ev[3].synchronize()
+        t_fwd = ev[0].elapsed_time(ev[1]) / args.time_steps
+        t_adj = ev[2].elapsed_time(ev[3]) / args.time_steps
+        t0 = time.perf_counter()
+        uT, grad = g.gradient(u0, nsteps, snaps, lambda uT: uT - target)
+        t_grad = time.perf_counter() - t0
+        st = g.gradient_stats()
+        res[prec] = {"forward_ms_per_step": t_fwd, "adjoint_ms_per_step": t_adj,
+                     "adjoint_over_forward": t_adj / t_fwd,
+                     "forward_GLUPs": cells / (t_fwd / 1e3) / 1e9, "adjoint_GLUPs": cells / (t_adj / 1e3) / 1e9,
+                     "gradient_seconds": t_grad, "gradient_forward_steps": st["forward_steps"],
+                     "gradient_adjoint_steps": st["adjoint_steps"], "grad": grad,
+                     "loss": 0.5 * float(np.vdot(uT - target, uT - target))}
+        g.close()
+    # central differences in FP64
+    fd_grid = Grid("heat3d", shape, "f64fast", U)
+
+    def loss(u):
+        fd_grid.upload(u)
+        fd_grid.forward(nsteps)
+        d = fd_grid.download() - target
+        return 0.5 * float(np.vdot(d, d))
+
+    rng = np.random.default_rng(2)
+    eps = 1e-6
+    errs64, errs32 = [], []
+    for _ in range(args.probes):
+        v = rng.standard_normal(u0.shape)
+        fd = (loss(u0 + eps * v) - loss(u0 - eps * v)) / (2 * eps)
+        errs64.append(abs(float(np.vdot(res["f64"]["grad"], v)) - fd) / abs(fd))
+        errs32.append(abs(float(np.vdot(res["f32"]["grad"], v)) - fd) / abs(fd))
+    fd_grid.close()
+    g32_vs_64 = W.rel_l2(res["f32"]["grad"], res["f64"]["grad"])
+    for p in res:
+        res[p].pop("grad")
+    line = {"metric": "GLUP/s", "value": res["f64"]["adjoint_GLUPs"], "unit": "GLUP/s",
+            "n_gpus": 1, "steps": args.time_steps, "warmup": 5, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {"workload": f"diffusion adjoint {n}^3 periodic, D*dt/dx^2=0.1, {nsteps} steps, "
+                                   f"32 Gaussians, binomial checkpointing {snaps} snapshots",
+                       "value_is": "adjoint step rate (FP64)"},
+            "adjoint": res,
+            "fd_check": {"probes": args.probes, "eps": eps, "max_rel_err_f64": max(errs64),
+                         "median_rel_err_f64": float(np.median(errs64)),
+                         "max_rel_err_f32": max(errs32), "median_rel_err_f32": float(np.median(errs32))},
+            "grad_f32_rel_l2_vs_f64": g32_vs_64}
+    print(json.dumps(line), flush=True)
+
+
+
+def run_batch(args):
+    """Batched Gray-Scott ensemble: 256 grids, sides log-uniform in
+    [64, 1024], F ~ U[0.02, 0.06], k ~ U[0.05, 0.065], 5000 steps, FP32
+    storage, persistent launches over one tile queue, time loop replayed
+    from a CUDA graph, kernel picked by the autotuner; against 256
+    sequential plain FP64 runs on the same GPU."""
+    import numpy as np
+    import torch
+    from formura_gb300 import build as B
+    if not os.path.exists(B.LIB):
+        B.build()
+    from formura_gb300 import workloads as W
+    from formura_gb300.host import Batch, Grid, builtin_program, program_uniforms
+    src, _ = builtin_program("gs2d")
+    members = W.ensemble(args.count, 0)
+    U, X = [], []
+    for i, (n, F, k) in enumerate(members):
+        _, u = program_uniforms(src, W.gs_config(n), "gs2d", params={"F": F, "kappa": k})
+        U.append(u)
+        X.append(W.gs_square_state(n, 1000 + i))
+    cells = sum(n * n for n, _, _ in members)
+    steps = args.batch_steps
+    b = Batch("gs2d", [(n, n) for n, _, _ in members], "f32", U)
+    for i, x in enumerate(X):
+        b.upload(i, x)
+    chosen = b.autotune(32)
+    kernel = b.variants()[chosen]
+    for i, x in enumerate(X):
+        b.upload(i, x)
+    stream = torch.cuda.ExternalStream(b.stream)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    sampler = ClockSampler(0)
+    sampler.start()
+    l0 = b.launches
+    b.synchronize()
+    e0.record(stream)
+    b.forward(steps)
+    e1.record(stream)
+    e1.synchronize()
+    clocks = sampler.stop()
+    ms = e0.elapsed_time(e1)
+    launches = b.launches - l0
+    f32_final = [b.download(i) for i in range(len(members))]
+    b.close()
+    value = cells * steps / (ms / 1e3) / 1e9
+    # 256 sequential plain FP64 runs (the bit-faithful drop-in kernels)
+    t0 = time.perf_counter()
+    errs = []
+    for i, (n, _, _) in enumerate(members):
+        g = Grid("gs2d", (n, n), "f64", U[i])
+        g.upload(X[i])
+        g.forward(steps)
+        f64 = g.download()
+        g.close()
+        errs.append(max(W.rel_l2(f32_final[i][j], f64[j]) for j in range(2)))
+    t64 = time.perf_counter() - t0
+    v64 = cells * steps / t64 / 1e9
+    line = {"metric": "GLUP/s", "value": value, "unit": "GLUP/s", "n_gpus": 1, "steps": 1,
+            "warmup": 1, "ms_per_step": ms, "higher_is_better": True, "scaling": "weak", "vs_baseline": None,
+            "dtype": "f32", "data": "synthetic",
+            "config": {"workload": f"batched gray-scott ensemble: {len(members)} grids, sides log-uniform "
+                                   f"[64,1024], F~U[.02,.06], k~U[.05,.065], {steps} steps",
+                       "cells_total": cells, "kernel": kernel,
+                       "launch": "persistent CTAs over one tile queue; 64-step chunks replayed from a CUDA graph"},
+            "gpu_launches": launches, "clocks": clocks,
+            "sequential_f64": {"value": v64, "unit": "GLUP/s", "seconds": t64,
+                               "note": "256 sequential fgb_open/forward/download runs, bit-faithful FP64"},
+            "speedup_vs_sequential_f64": value / v64,
+            "rel_l2_f32_vs_f64": {"median": float(np.median(errs)), "max": float(np.max(errs))}}
+    print(json.dumps(line), flush=True)
 
 
 if __name__ == "__main__":

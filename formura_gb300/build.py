@@ -53,6 +53,11 @@ def runtime_params(cfg_text: str) -> List[str]:
     return [str(x) for x in v]
 
 
+def library_runtime_params(name: str) -> List[str]:
+    """Runtime parameters the library's kernels of `name` were compiled with."""
+    return runtime_params(program_sources(name)[1])
+
+
 def generate(names: Optional[List[str]] = None) -> Dict[str, str]:
     """Emit device code for each program; return name -> .cu path."""
     from .generator.config import decode_config
@@ -122,6 +127,7 @@ def build(names: Optional[List[str]] = None, jobs: Optional[int] = None, verbose
             if os.path.exists(os.path.join(CSRC, f))] + [os.path.join(ROOT, "include", "formura_gb300.h")]
     units = [(os.path.join(CSRC, "fgb_runtime.cu"), os.path.join(BUILD, "fgb_runtime.o")),
              (os.path.join(CSRC, "fgb_noalloc.cu"), os.path.join(BUILD, "fgb_noalloc.o")),
+             (os.path.join(CSRC, "fgb_batch.cu"), os.path.join(BUILD, "fgb_batch.o")),
              (os.path.join(GEN, "fgb_registry.cu"), os.path.join(BUILD, "fgb_registry.o"))]
     units += [(p, os.path.join(BUILD, f"prog_{n}.o")) for n, p in gen.items()]
     jobs = jobs or max(2, min(len(units), os.cpu_count() or 4))

@@ -1,0 +1,277 @@
+// Temporal blocking on the GPU: K time steps per launch inside a shared-memory
+// tile, for programs whose step is a single stage (every manifest value is a
+// store).  This replaces the reference's CPU temporal blocking
+// (Templates.hs:311-381: floor/wall buffers walked block by block): each
+// CTA loads its output tile plus a halo of K*R cells (R: how far the stencil
+// reads) with periodic wrap, advances K steps in shared memory, shrinking the
+// valid region by R per step, and writes the tile rolled by K*shift.  The
+// same generated stage functor runs per cell, so the result is bit-identical
+// to K single steps of the generic kernel.
+#pragma once
+#include "fgb_templates.cuh"
+
+namespace fgb {
+
+// Accessor over a shared-memory tile: cursor loads read the current buffer,
+// stores write the next one.  Layout [field][row][col], col contiguous.
+template <class T, int NF, int RY, int RX>
+struct TileAccess {
+  const T* cur;
+  T* nxt;
+  int ly, lx;
+  template <int F, int D0, int D1, int D2>
+  __device__ __forceinline__ T ld() const {
+    static_assert(D0 == 0, "2D tile");
+    return cur[(F * RY + ly + D1) * RX + lx + D2];
+  }
+  template <int F>
+  __device__ __forceinline__ void st(T v) const {
+    nxt[(F * RY + ly) * RX + lx] = v;
+  }
+};
+
+// Same tile, but stores go to registers: a thread computes several rows of
+// one column before writing any of them, so loads shared between the rows
+// (the vertical neighbours) are read from shared memory once.
+template <class T, int NF, int RY, int RX>
+struct RegTileAccess {
+  const T* cur;
+  T* res;
+  int ly, lx;
+  template <int F, int D0, int D1, int D2>
+  __device__ __forceinline__ T ld() const {
+    static_assert(D0 == 0, "2D tile");
+    return cur[(F * RY + ly + D1) * RX + lx + D2];
+  }
+  template <int F>
+  __device__ __forceinline__ void st(T v) const {
+    res[F] = v;
+  }
+};
+
+__device__ __forceinline__ int pmod(int a, int n) {
+  int r = a % n;
+  return r < 0 ? r + n : r;
+}
+
+template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY, int RB>
+__global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ FgbLaunch L) {
+  using T = typename M::T;
+  constexpr int NF = Prog::kFields;
+  constexpr int R = Prog::kReach;
+  constexpr int H = K * R;
+  constexpr int RY = TY + 2 * H, RX = TX + 2 * H;
+  constexpr int PLANE = RY * RX;
+  extern __shared__ __align__(16) unsigned char fgb_smem_raw[];
+  T* smem = reinterpret_cast<T*>(fgb_smem_raw);
+  const int ny = L.n[1], nx = L.n[2];
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  const T* __restrict__ U = static_cast<const T*>(L.uniforms);
+
+  // load the tile and its halo (periodic)
+  for (int ly = threadIdx.y; ly < RY; ly += BY) {
+    const int gy = pmod(y0 - H + ly, ny);
+    for (int lx = threadIdx.x; lx < RX; lx += BX) {
+      const int gx = pmod(x0 - H + lx, nx);
+      const uint32_t g = (uint32_t)gy * (uint32_t)nx + (uint32_t)gx;
+#pragma unroll
+      for (int f = 0; f < NF; ++f)
+        smem[f * PLANE + ly * RX + lx] = Storage<S, T>::load(static_cast<const S*>(L.in[f])[g], L.scale[f]);
+    }
+  }
+  __syncthreads();
+
+#pragma unroll 1
+  for (int k = 0; k < K; ++k) {
+    const T* cur = smem + (k & 1) * NF * PLANE;
+    T* nxt = smem + ((k + 1) & 1) * NF * PLANE;
+    const int lo = (k + 1) * R;
+    if constexpr (RB == 1) {
+      for (int ly = lo + threadIdx.y; ly < RY - lo; ly += BY) {
+        for (int lx = lo + threadIdx.x; lx < RX - lo; lx += BX) {
+          TileAccess<T, NF, RY, RX> a{cur, nxt, ly, lx};
+          Stage::template run<M>(a, U);
+        }
+      }
+    } else {
+      const int last = RY - lo - 1;   // rows past the region are clamped (computed, not stored)
+      for (int ly0 = lo + threadIdx.y * RB; ly0 <= last; ly0 += BY * RB) {
+        for (int lx = lo + threadIdx.x; lx < RX - lo; lx += BX) {
+          T res[RB][NF];
+#pragma unroll
+          for (int r = 0; r < RB; ++r) {
+            RegTileAccess<T, NF, RY, RX> a{cur, res[r], min(ly0 + r, last), lx};
+            Stage::template run<M>(a, U);
+          }
+#pragma unroll
+          for (int r = 0; r < RB; ++r) {
+            if (ly0 + r <= last) {
+#pragma unroll
+              for (int f = 0; f < NF; ++f) nxt[(f * RY + ly0 + r) * RX + lx] = res[r][f];
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+
+  // store the tile, rolled by K steps' worth of shift
+  const T* fin = smem + (K & 1) * NF * PLANE;
+  for (int ty = threadIdx.y; ty < TY; ty += BY) {
+    const int py = y0 + ty;
+    if (py >= ny) break;
+    const int oy = (py + K * Prog::kShift) % ny;
+    for (int tx = threadIdx.x; tx < TX; tx += BX) {
+      const int px = x0 + tx;
+      if (px >= nx) break;
+      const int ox = (px + K * Prog::kShift) % nx;
+      const uint32_t g = (uint32_t)oy * (uint32_t)nx + (uint32_t)ox;
+#pragma unroll
+      for (int f = 0; f < NF; ++f)
+        static_cast<S*>(L.out[f])[g] =
+            Storage<S, T>::store(fin[f * PLANE + (ty + H) * RX + tx + H], L.inv_scale[f]);
+    }
+  }
+}
+
+template <class Prog, int P, class Stage, int TX, int TY, int K, int RB = 1>
+struct Tb2dVariant {
+  using M = typename Precision<P>::M;
+  using S = typename Precision<P>::S;
+  using T = typename M::T;
+  static constexpr int BX = 32, BY = 8;
+  static constexpr int H = K * Prog::kReach;
+  static constexpr size_t kSmem = (size_t)2 * Prog::kFields * (TY + 2 * H) * (TX + 2 * H) * sizeof(T);
+
+  static cudaError_t launch(const FgbLaunch* L, cudaStream_t stream) {
+    auto kern = tb2d_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY, RB>;
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    dim3 grid((L->n[2] + TX - 1) / TX, (L->n[1] + TY - 1) / TY, 1);
+    kern<<<grid, dim3(BX, BY), kSmem, stream>>>(*L);
+    return cudaGetLastError();
+  }
+  static FgbFusedVariant describe() {
+    FgbFusedVariant v;
+    v.launch = &launch;
+    v.tile_x = TX;
+    v.tile_y = TY;
+    v.steps = K;
+    v.smem_bytes = kSmem;
+    return v;
+  }
+};
+
+// Batched ensemble: persistent CTAs walk a queue of tiles drawn from every
+// grid of the batch; each tile advances K steps in shared memory exactly like
+// tb2d_kernel, with that grid's extent, periodic wrap and uniform table.
+template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY>
+__global__ void __launch_bounds__(BX * BY) tb2d_batch_kernel(const __grid_constant__ FgbBatchLaunch B) {
+  using T = typename M::T;
+  constexpr int NF = Prog::kFields;
+  constexpr int R = Prog::kReach;
+  constexpr int H = K * R;
+  constexpr int RY = TY + 2 * H, RX = TX + 2 * H;
+  constexpr int PLANE = RY * RX;
+  extern __shared__ __align__(16) unsigned char fgb_smem_raw[];
+  T* smem = reinterpret_cast<T*>(fgb_smem_raw);
+  for (int t = blockIdx.x; t < B.ntiles; t += gridDim.x) {
+    const FgbBatchTile tile = B.tiles[t];
+    const FgbBatchInstance in = B.inst[tile.inst];
+    const int ny = in.ny, nx = in.nx;
+    const size_t cells = (size_t)ny * nx;
+    const S* src = static_cast<const S*>(in.state[B.parity]);
+    S* dst = static_cast<S*>(in.state[B.parity ^ 1]);
+    const T* __restrict__ U = static_cast<const T*>(in.uniforms);
+    const int x0 = tile.x0, y0 = tile.y0;
+    for (int ly = threadIdx.y; ly < RY; ly += BY) {
+      const int gy = pmod(y0 - H + ly, ny);
+      for (int lx = threadIdx.x; lx < RX; lx += BX) {
+        const int gx = pmod(x0 - H + lx, nx);
+        const size_t g = (size_t)gy * nx + gx;
+#pragma unroll
+        for (int f = 0; f < NF; ++f)
+          smem[f * PLANE + ly * RX + lx] = Storage<S, T>::load(src[f * cells + g], 1.0f);
+      }
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int k = 0; k < K; ++k) {
+      const T* cur = smem + (k & 1) * NF * PLANE;
+      T* nxt = smem + ((k + 1) & 1) * NF * PLANE;
+      const int lo = (k + 1) * R;
+      for (int ly = lo + threadIdx.y; ly < RY - lo; ly += BY) {
+        for (int lx = lo + threadIdx.x; lx < RX - lo; lx += BX) {
+          TileAccess<T, NF, RY, RX> a{cur, nxt, ly, lx};
+          Stage::template run<M>(a, U);
+        }
+      }
+      __syncthreads();
+    }
+    const T* fin = smem + (K & 1) * NF * PLANE;
+    for (int ty = threadIdx.y; ty < TY; ty += BY) {
+      const int py = y0 + ty;
+      if (py >= ny) break;
+      const int oy = (py + K * Prog::kShift) % ny;
+      for (int tx = threadIdx.x; tx < TX; tx += BX) {
+        const int px = x0 + tx;
+        if (px >= nx) break;
+        const int ox = (px + K * Prog::kShift) % nx;
+        const size_t g = (size_t)oy * nx + ox;
+#pragma unroll
+        for (int f = 0; f < NF; ++f)
+          dst[f * cells + g] = Storage<S, T>::store(fin[f * PLANE + (ty + H) * RX + tx + H], 1.0f);
+      }
+    }
+    __syncthreads();   // the next tile reuses the shared buffers
+  }
+}
+
+template <class Prog, int P, class Stage, int TX, int TY, int K>
+struct Tb2dBatchVariant {
+  using M = typename Precision<P>::M;
+  using S = typename Precision<P>::S;
+  using T = typename M::T;
+  static constexpr int BX = 32, BY = 8;
+  static constexpr int H = K * Prog::kReach;
+  static constexpr size_t kSmem = (size_t)2 * Prog::kFields * (TY + 2 * H) * (TX + 2 * H) * sizeof(T);
+
+  static cudaError_t configure() {
+    static cudaError_t state = cudaErrorNotReady;
+    if (state == cudaErrorNotReady)
+      state = cudaFuncSetAttribute(tb2d_batch_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY>,
+                                   cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+    return state;
+  }
+  static cudaError_t launch(const FgbBatchLaunch* B, cudaStream_t stream, int blocks) {
+    cudaError_t e = configure();
+    if (e != cudaSuccess) return e;
+    tb2d_batch_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY><<<blocks, dim3(BX, BY), kSmem, stream>>>(*B);
+    return cudaGetLastError();
+  }
+  static int blocks_per_sm() {
+    if (configure() != cudaSuccess) return 0;
+    int n = 0;
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, tb2d_batch_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY>,
+                                                      BX * BY, kSmem) != cudaSuccess)
+      return 0;
+    return n;
+  }
+  static FgbBatchVariant describe() {
+    FgbBatchVariant v;
+    v.launch = &launch;
+    v.blocks_per_sm = &blocks_per_sm;
+    v.tile_x = TX;
+    v.tile_y = TY;
+    v.steps = K;
+    v.smem_bytes = kSmem;
+    return v;
+  }
+};
+
+}  // namespace fgb

@@ -24,17 +24,55 @@ struct FgbLaunch {
   int fused_steps;                  // >1: temporal blocking inside one launch
 };
 
+#define FGB_MAX_FUSED 8
+
 typedef cudaError_t (*FgbStageLaunch)(const FgbLaunch* args, cudaStream_t stream);
-// Fused multi-step launch for single-stage programs (nullptr when absent).
-typedef cudaError_t (*FgbFusedLaunch)(const FgbLaunch* args, cudaStream_t stream);
+
+// One temporal-blocking kernel: `steps` time steps per launch on tiles of
+// tile_x x tile_y output cells (single-stage programs only).
+struct FgbFusedVariant {
+  FgbStageLaunch launch;
+  int tile_x, tile_y, steps;
+  size_t smem_bytes;
+};
+
+// Batched ensembles: many independent 2D grids of one single-stage program,
+// each with its own extent and uniform table, advanced together.
+struct FgbBatchInstance {
+  void* state[2];          // the two state buffers (fields back to back)
+  const void* uniforms;    // this grid's uniform table (compute type)
+  int ny, nx;              // extent; x is the contiguous axis
+};
+struct FgbBatchTile {
+  int inst, y0, x0, pad;
+};
+struct FgbBatchLaunch {
+  const FgbBatchInstance* inst;
+  const FgbBatchTile* tiles;
+  int ntiles;
+  int parity;              // state buffer read by this launch
+};
+typedef cudaError_t (*FgbBatchFn)(const FgbBatchLaunch* args, cudaStream_t stream, int blocks);
+typedef int (*FgbOccupancyFn)(void);
+struct FgbBatchVariant {
+  FgbBatchFn launch;
+  FgbOccupancyFn blocks_per_sm;
+  int tile_x, tile_y, steps;
+  size_t smem_bytes;
+};
 
 struct FgbProgramDesc {
   const char* name;
   int dim, nfields, nmids, nstages, sleeve, shift, reach, nuniforms;
   const char* const* field_names;
   FgbStageLaunch launch[FGB_NUM_PRECISIONS][FGB_MAX_STAGES];
-  FgbFusedLaunch fused[FGB_NUM_PRECISIONS];
-  int fused_max_steps;
+  FgbFusedVariant fused[FGB_NUM_PRECISIONS][FGB_MAX_FUSED];
+  int nfused[FGB_NUM_PRECISIONS];
+  // Adjoint step (transpose of the step's Jacobian), single-stage programs:
+  // in = forward state u_n, mid[f] = lambda_{n+1}, out = lambda_n.
+  FgbStageLaunch adjoint[FGB_NUM_PRECISIONS];
+  FgbBatchVariant batch[FGB_NUM_PRECISIONS][FGB_MAX_FUSED];
+  int nbatch[FGB_NUM_PRECISIONS];
 };
 
 typedef const FgbProgramDesc* (*FgbProgramGetter)(void);

@@ -7,6 +7,7 @@
 #include <stdarg.h>
 #include <stdio.h>
 #include <string.h>
+#include <algorithm>
 #include <string>
 #include <vector>
 
@@ -92,6 +93,13 @@ struct fgb_grid {
   int64_t launches = 0;
   cudaGraphExec_t graph = nullptr;      // a chunk of kGraphSteps steps
   int graph_cur = -1;
+  int variant = -1;                     // temporal-blocking kernel in use, -1: one step per launch
+  // reverse mode
+  void* lam[2] = {nullptr, nullptr};    // adjoint state, storage precision
+  int lcur = 0;
+  std::vector<void*> snaps;             // checkpoints of the forward state
+  int grad_steps = -1;                  // steps recorded by fgb_gradient_forward
+  int64_t grad_fwd = 0, grad_adj = 0;   // forward steps (incl. recomputation) and adjoint steps
 };
 
 static const int kGraphSteps = 16;
@@ -115,6 +123,16 @@ static int run_steps(fgb_grid* g, int nsteps) {
   FgbLaunch L[2];
   fill_launch(g, 0, &L[0]);
   fill_launch(g, 1, &L[1]);
+  if (g->variant >= 0) {
+    const FgbFusedVariant& v = g->prog->fused[g->precision][g->variant];
+    while (nsteps >= v.steps) {
+      cudaError_t e = v.launch(&L[g->cur], g->stream);
+      if (e != cudaSuccess) return cuda_fail(e, "fused launch");
+      ++g->launches;
+      g->cur ^= 1;
+      nsteps -= v.steps;
+    }
+  }
   for (int s = 0; s < nsteps; ++s) {
     for (int st = 0; st < g->prog->nstages; ++st) {
       cudaError_t e = g->prog->launch[g->precision][st](&L[g->cur], g->stream);
@@ -127,6 +145,8 @@ static int run_steps(fgb_grid* g, int nsteps) {
 }
 
 extern "C" {
+
+static void free_snaps(fgb_grid* g);
 
 const char* fgb_last_error(void) { return g_last_error.c_str(); }
 
@@ -221,6 +241,9 @@ int fgb_close(fgb_grid* g) {
   cudaFree(g->mids);
   cudaFree(g->uniforms);
   cudaFree(g->staging);
+  cudaFree(g->lam[0]);
+  cudaFree(g->lam[1]);
+  free_snaps(g);
   if (g->stream) cudaStreamDestroy(g->stream);
   delete g;
   return FGB_OK;
@@ -317,6 +340,291 @@ int fgb_forward(fgb_grid* g, int nsteps) {
     }
   }
   return run_steps(g, nsteps - done);
+}
+
+int fgb_variant_count(fgb_grid* g) { return g ? g->prog->nfused[g->precision] : 0; }
+
+int fgb_variant_info(fgb_grid* g, int index, int* tile_x, int* tile_y, int* steps) {
+  if (!g || index < 0 || index >= g->prog->nfused[g->precision]) return fail(FGB_E_ARG, "no such variant");
+  const FgbFusedVariant& v = g->prog->fused[g->precision][index];
+  if (tile_x) *tile_x = v.tile_x;
+  if (tile_y) *tile_y = v.tile_y;
+  if (steps) *steps = v.steps;
+  return FGB_OK;
+}
+
+static bool variant_fits(const fgb_grid* g, int index) {
+  int dev = 0, optin = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+  return g->prog->fused[g->precision][index].smem_bytes <= (size_t)optin;
+}
+
+int fgb_set_variant(fgb_grid* g, int index) {
+  if (!g || index < -1 || index >= g->prog->nfused[g->precision]) return fail(FGB_E_ARG, "no such variant");
+  if (index >= 0 && !variant_fits(g, index))
+    return fail(FGB_E_ARG, "variant %d needs %zu bytes of shared memory", index,
+                g->prog->fused[g->precision][index].smem_bytes);
+  if (index != g->variant && g->graph) {
+    cudaGraphExecDestroy(g->graph);
+    g->graph = nullptr;
+  }
+  g->variant = index;
+  return FGB_OK;
+}
+
+int fgb_variant(fgb_grid* g) { return g ? g->variant : -1; }
+
+int fgb_autotune(fgb_grid* g, int trial_steps, int* chosen) {
+  if (!g || trial_steps < 8) return fail(FGB_E_ARG, "autotune needs a grid and at least 8 trial steps");
+  const int nv = g->prog->nfused[g->precision];
+  if (nv == 0) {
+    if (chosen) *chosen = -1;
+    return fgb_set_variant(g, -1);
+  }
+  const size_t bytes = g->cells * g->prog->nfields * storage_size(g->precision);
+  void* backup = nullptr;
+  FGB_CUDA(cudaMalloc(&backup, bytes), "autotune backup");
+  FGB_CUDA(cudaMemcpyAsync(backup, g->state[g->cur], bytes, cudaMemcpyDeviceToDevice, g->stream), "autotune");
+  const int64_t launches0 = g->launches;
+  const int old_variant = g->variant;
+  cudaEvent_t e0, e1;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  float best = 0.0f;
+  int best_i = -1;
+  int rc = FGB_OK;
+  for (int i = -1; i < nv && rc == FGB_OK; ++i) {
+    if (i >= 0 && !variant_fits(g, i)) continue;
+    g->variant = i;
+    const int k = i >= 0 ? g->prog->fused[g->precision][i].steps : 1;
+    const int steps = ((trial_steps + k - 1) / k) * k;
+    rc = run_steps(g, k);                       // warm-up (and kernel attribute set-up)
+    if (rc != FGB_OK) break;
+    cudaEventRecord(e0, g->stream);
+    rc = run_steps(g, steps);
+    cudaEventRecord(e1, g->stream);
+    if (cudaEventSynchronize(e1) != cudaSuccess) rc = cuda_fail(cudaGetLastError(), "autotune");
+    float ms = 0.0f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const float per_step = ms / steps;
+    if (rc == FGB_OK && (i == -1 || per_step < best)) {
+      best = per_step;
+      best_i = i;
+    }
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaMemcpyAsync(g->state[g->cur], backup, bytes, cudaMemcpyDeviceToDevice, g->stream);
+  cudaStreamSynchronize(g->stream);
+  cudaFree(backup);
+  g->launches = launches0;
+  g->variant = old_variant;
+  if (rc != FGB_OK) return rc;
+  if (chosen) *chosen = best_i;
+  return fgb_set_variant(g, best_i);
+}
+
+// ---------------------------------------------------------------------------
+// reverse mode: adjoint steps and checkpointed gradients
+// ---------------------------------------------------------------------------
+static size_t state_bytes(const fgb_grid* g) { return g->cells * g->prog->nfields * storage_size(g->precision); }
+
+static int ensure_adjoint(fgb_grid* g) {
+  if (!g->prog->adjoint[g->precision])
+    return fail(FGB_E_ARG, "program %s has no adjoint in this precision", g->prog->name);
+  for (int b = 0; b < 2; ++b)
+    if (!g->lam[b]) FGB_CUDA(cudaMalloc(&g->lam[b], state_bytes(g)), "adjoint state");
+  return FGB_OK;
+}
+
+// host FP64 (formura_data layout) <-> device state in storage precision
+static int host_to_state(fgb_grid* g, const double* host, void* dst) {
+  const size_t n = g->cells * g->prog->nfields;
+  if (g->precision <= FGB_F64_FAST) {
+    FGB_CUDA(cudaMemcpyAsync(dst, host, n * 8, cudaMemcpyHostToDevice, g->stream), "copy in");
+  } else {
+    FGB_CUDA(cudaMemcpyAsync(g->staging, host, n * 8, cudaMemcpyHostToDevice, g->stream), "copy in");
+    if (g->precision == FGB_F32) to_storage<float><<<1024, 256, 0, g->stream>>>(g->staging, (float*)dst, n, 1.0f);
+    else to_storage<__half><<<1024, 256, 0, g->stream>>>(g->staging, (__half*)dst, n, 1.0f);
+    ++g->launches;
+    FGB_CUDA(cudaGetLastError(), "copy in");
+  }
+  return FGB_OK;
+}
+
+static int state_to_host(fgb_grid* g, const void* src, double* host) {
+  const size_t n = g->cells * g->prog->nfields;
+  if (g->precision <= FGB_F64_FAST) {
+    FGB_CUDA(cudaMemcpyAsync(host, src, n * 8, cudaMemcpyDeviceToHost, g->stream), "copy out");
+  } else {
+    if (g->precision == FGB_F32) from_storage<float><<<1024, 256, 0, g->stream>>>((const float*)src, g->staging, n, 1.0f);
+    else from_storage<__half><<<1024, 256, 0, g->stream>>>((const __half*)src, g->staging, n, 1.0f);
+    ++g->launches;
+    FGB_CUDA(cudaGetLastError(), "copy out");
+    FGB_CUDA(cudaMemcpyAsync(host, g->staging, n * 8, cudaMemcpyDeviceToHost, g->stream), "copy out");
+  }
+  FGB_CUDA(cudaStreamSynchronize(g->stream), "copy out");
+  return FGB_OK;
+}
+
+// lambda <- (dF/du at `u`)^T lambda
+static int adjoint_step(fgb_grid* g, const void* u) {
+  FgbLaunch L;
+  fill_launch(g, g->cur, &L);
+  const size_t es = storage_size(g->precision);
+  for (int f = 0; f < g->prog->nfields; ++f) {
+    L.in[f] = (const char*)u + f * g->cells * es;
+    L.mid[f] = (char*)g->lam[g->lcur] + f * g->cells * es;
+    L.out[f] = (char*)g->lam[g->lcur ^ 1] + f * g->cells * es;
+  }
+  cudaError_t e = g->prog->adjoint[g->precision](&L, g->stream);
+  if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
+  ++g->launches;
+  ++g->grad_adj;
+  g->lcur ^= 1;
+  return FGB_OK;
+}
+
+static int64_t binom(int s, int t) {   // C(s + t, s), saturating
+  double r = 1.0;
+  for (int i = 1; i <= s; ++i) r = r * (t + i) / i;
+  return r > 4e18 ? (int64_t)4e18 : (int64_t)(r + 0.5);
+}
+
+struct Reversal {
+  fgb_grid* g;
+  std::vector<int> free_slots;
+  size_t bytes;
+
+  int restore(int slot) {
+    FGB_CUDA(cudaMemcpyAsync(g->state[g->cur], g->snaps[slot], bytes, cudaMemcpyDeviceToDevice, g->stream),
+             "restore checkpoint");
+    return FGB_OK;
+  }
+  int advance(int n) {
+    g->grad_fwd += n;
+    return run_steps(g, n);
+  }
+  // u_l is in checkpoint `slot`; lambda holds lambda_r; leaves lambda_l.
+  int reverse(int l, int r, int slot) {
+    int rc;
+    if (r - l == 1) {
+      if ((rc = restore(slot)) != FGB_OK) return rc;
+      return adjoint_step(g, g->state[g->cur]);
+    }
+    const int s = (int)free_slots.size();
+    if (s == 0) {
+      // no free checkpoint: recompute each state from u_l
+      for (int k = r - 1; k >= l; --k) {
+        if ((rc = restore(slot)) != FGB_OK) return rc;
+        if ((rc = advance(k - l)) != FGB_OK) return rc;
+        if ((rc = adjoint_step(g, g->state[g->cur])) != FGB_OK) return rc;
+      }
+      return FGB_OK;
+    }
+    // binomial split: [m, r) is reversed with s-1 free checkpoints and
+    // [l, m) with s, each within t sweeps (Griewank's revolve bound)
+    int t = 1;
+    while (binom(s, t) < r - l) ++t;
+    int m = r - (int)std::min<int64_t>(binom(s - 1, t), r - l - 1);
+    if (m <= l) m = l + 1;
+    if ((rc = restore(slot)) != FGB_OK) return rc;
+    if ((rc = advance(m - l)) != FGB_OK) return rc;
+    const int sm = free_slots.back();
+    free_slots.pop_back();
+    FGB_CUDA(cudaMemcpyAsync(g->snaps[sm], g->state[g->cur], bytes, cudaMemcpyDeviceToDevice, g->stream),
+             "store checkpoint");
+    rc = reverse(m, r, sm);
+    free_slots.push_back(sm);
+    if (rc != FGB_OK) return rc;
+    return reverse(l, m, slot);
+  }
+};
+
+static void free_snaps(fgb_grid* g) {
+  for (void* p : g->snaps) cudaFree(p);
+  g->snaps.clear();
+}
+
+int fgb_backward(fgb_grid* g, const double* lambda_next, double* lambda) {
+  if (!g || !lambda_next || !lambda) return fail(FGB_E_ARG, "null argument");
+  int rc = ensure_adjoint(g);
+  if (rc != FGB_OK) return rc;
+  if ((rc = host_to_state(g, lambda_next, g->lam[g->lcur])) != FGB_OK) return rc;
+  if ((rc = adjoint_step(g, g->state[g->cur])) != FGB_OK) return rc;
+  return state_to_host(g, g->lam[g->lcur], lambda);
+}
+
+int fgb_adjoint_steps(fgb_grid* g, int nsteps) {
+  if (!g || nsteps < 0) return fail(FGB_E_ARG, "bad arguments");
+  int rc = ensure_adjoint(g);
+  for (int i = 0; i < nsteps && rc == FGB_OK; ++i) rc = adjoint_step(g, g->state[g->cur]);
+  return rc;
+}
+
+int fgb_gradient_forward(fgb_grid* g, int nsteps, int snapshots) {
+  if (!g || nsteps < 1 || snapshots < 1) return fail(FGB_E_ARG, "need nsteps >= 1 and snapshots >= 1");
+  int rc = ensure_adjoint(g);
+  if (rc != FGB_OK) return rc;
+  free_snaps(g);
+  for (int i = 0; i < snapshots; ++i) {
+    void* p = nullptr;
+    cudaError_t e = cudaMalloc(&p, state_bytes(g));
+    if (e != cudaSuccess) {
+      free_snaps(g);
+      return cuda_fail(e, "checkpoint buffers");
+    }
+    g->snaps.push_back(p);
+  }
+  FGB_CUDA(cudaMemcpyAsync(g->snaps[0], g->state[g->cur], state_bytes(g), cudaMemcpyDeviceToDevice, g->stream),
+           "checkpoint u0");
+  g->grad_fwd = nsteps;
+  g->grad_adj = 0;
+  g->grad_steps = nsteps;
+  return run_steps(g, nsteps);
+}
+
+static int gradient_backward(fgb_grid* g) {
+  if (g->grad_steps < 1) return fail(FGB_E_ARG, "fgb_gradient_forward was not called");
+  Reversal R{g, {}, state_bytes(g)};
+  for (int i = (int)g->snaps.size() - 1; i >= 1; --i) R.free_slots.push_back(i);
+  int rc = R.reverse(0, g->grad_steps, 0);
+  if (rc == FGB_OK) rc = R.restore(0);          // the state is u_0 again
+  g->grad_steps = -1;
+  if (rc == FGB_OK) {
+    cudaError_t e = cudaStreamSynchronize(g->stream);
+    if (e != cudaSuccess) rc = cuda_fail(e, "gradient");
+  }
+  free_snaps(g);
+  return rc;
+}
+
+int fgb_gradient_backward(fgb_grid* g, const double* seed, double* grad) {
+  if (!g || !seed || !grad) return fail(FGB_E_ARG, "null argument");
+  int rc = ensure_adjoint(g);
+  if (rc != FGB_OK) return rc;
+  if ((rc = host_to_state(g, seed, g->lam[g->lcur])) != FGB_OK) return rc;
+  if ((rc = gradient_backward(g)) != FGB_OK) return rc;
+  return state_to_host(g, g->lam[g->lcur], grad);
+}
+
+int fgb_gradient_backward_device(fgb_grid* g, const void* seed, void* grad) {
+  if (!g || !seed || !grad) return fail(FGB_E_ARG, "null argument");
+  int rc = ensure_adjoint(g);
+  if (rc != FGB_OK) return rc;
+  FGB_CUDA(cudaMemcpyAsync(g->lam[g->lcur], seed, state_bytes(g), cudaMemcpyDeviceToDevice, g->stream), "seed");
+  if ((rc = gradient_backward(g)) != FGB_OK) return rc;
+  FGB_CUDA(cudaMemcpyAsync(grad, g->lam[g->lcur], state_bytes(g), cudaMemcpyDeviceToDevice, g->stream), "gradient");
+  FGB_CUDA(cudaStreamSynchronize(g->stream), "gradient");
+  return FGB_OK;
+}
+
+int fgb_gradient_stats(fgb_grid* g, int64_t* forward_steps, int64_t* adjoint_steps) {
+  if (!g) return fail(FGB_E_ARG, "null grid");
+  if (forward_steps) *forward_steps = g->grad_fwd;
+  if (adjoint_steps) *adjoint_steps = g->grad_adj;
+  return FGB_OK;
 }
 
 int fgb_synchronize(fgb_grid* g) {

@@ -7,6 +7,7 @@
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <stdint.h>
+#include <type_traits>
 #include "fgb_internal.h"
 
 namespace fgb {
@@ -163,6 +164,42 @@ struct GlobalAccess {
   }
 };
 
+// Accessor of the adjoint kernel: the forward state u_n at q + D (in),
+// the adjoint state lambda_{n+1} at q + D (mid[f]) and the new adjoint
+// lambda_n at q (out).  No roll: the roll is folded into the cursors of the
+// lambda loads by the generator.
+template <class S, class T>
+struct AdjointAccess {
+  const FgbLaunch& L;
+  int p0, p1, p2;
+
+  __device__ __forceinline__ uint32_t lin(int i0, int i1, int i2) const {
+    return ((uint32_t)i0 * (uint32_t)L.n[1] + (uint32_t)i1) * (uint32_t)L.n[2] + (uint32_t)i2;
+  }
+  __device__ __forceinline__ static int wrapv(int p, int d, int n) {
+    int i = p + d;
+    while (i < 0) i += n;
+    while (i >= n) i -= n;
+    return i;
+  }
+  template <int F, int D0, int D1, int D2>
+  __device__ __forceinline__ T ld() const {
+    const S* a = static_cast<const S*>(L.in[F]);
+    return Storage<S, T>::load(a[lin(wrapv(p0, D0, L.n[0]), wrapv(p1, D1, L.n[1]), wrapv(p2, D2, L.n[2]))],
+                               L.scale[F]);
+  }
+  template <int F, int D0, int D1, int D2>
+  __device__ __forceinline__ T ldl() const {
+    const S* a = static_cast<const S*>(L.mid[F]);
+    return Storage<S, T>::load(a[lin(wrapv(p0, D0, L.n[0]), wrapv(p1, D1, L.n[1]), wrapv(p2, D2, L.n[2]))],
+                               1.0f);
+  }
+  template <int F>
+  __device__ __forceinline__ void stl(T v) const {
+    static_cast<S*>(L.out[F])[lin(p0, p1, p2)] = Storage<S, T>::store(v, 1.0f);
+  }
+};
+
 constexpr int kBlockX = 128;
 
 // One thread per grid point; x covers the contiguous (last) axis.
@@ -174,6 +211,24 @@ __global__ void __launch_bounds__(kBlockX) stage_kernel(const __grid_constant__ 
   Stage::template run<M>(a, static_cast<const typename M::T*>(L.uniforms));
 }
 
+template <class M, class S, class Adj>
+__global__ void __launch_bounds__(kBlockX) adjoint_kernel(const __grid_constant__ FgbLaunch L) {
+  const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p2 >= L.n[2]) return;
+  AdjointAccess<S, typename M::T> a{L, (int)blockIdx.z, (int)blockIdx.y, p2};
+  Adj::template run<M>(a, static_cast<const typename M::T*>(L.uniforms));
+}
+
+template <int P, class Adj>
+cudaError_t launch_adjoint(const FgbLaunch* L, cudaStream_t stream) {
+  using M = typename Precision<P>::M;
+  using S = typename Precision<P>::S;
+  const int bx = L->n[2] >= kBlockX ? kBlockX : ((L->n[2] + 31) / 32) * 32;
+  dim3 grid((L->n[2] + bx - 1) / bx, L->n[1], L->n[0]);
+  adjoint_kernel<M, S, Adj><<<grid, bx, 0, stream>>>(*L);
+  return cudaGetLastError();
+}
+
 template <class Prog, int P, class Stage>
 cudaError_t launch_stage(const FgbLaunch* L, cudaStream_t stream) {
   using M = typename Precision<P>::M;
@@ -183,6 +238,64 @@ cudaError_t launch_stage(const FgbLaunch* L, cudaStream_t stream) {
   stage_kernel<M, S, Prog::kDim, Prog::kShift, Stage><<<grid, bx, 0, stream>>>(*L);
   return cudaGetLastError();
 }
+
+template <class Prog, class... Stages>
+struct ProgramBuilder;
+}  // namespace fgb
+#include "fgb_fused.cuh"
+namespace fgb {
+
+template <class Prog, class Stage0, class... Rest>
+struct FusedFill {
+  template <int P>
+  static void fill(FgbProgramDesc& d) {
+    if constexpr (Prog::kDim == 2 && Prog::kStages == 1 && Prog::kMids == 0) {
+      const FgbFusedVariant v[] = {
+          Tb2dVariant<Prog, P, Stage0, 64, 32, 2>::describe(),
+          Tb2dVariant<Prog, P, Stage0, 64, 32, 4>::describe(),
+          Tb2dVariant<Prog, P, Stage0, 64, 64, 4>::describe(),
+          Tb2dVariant<Prog, P, Stage0, 128, 32, 4>::describe(),
+          Tb2dVariant<Prog, P, Stage0, 64, 32, 4, 4>::describe(),
+          Tb2dVariant<Prog, P, Stage0, 64, 64, 4, 4>::describe(),
+          Tb2dVariant<Prog, P, Stage0, 128, 64, 8, 4>::describe(),
+          Tb2dVariant<Prog, P, Stage0, 64, 64, 8, 2>::describe(),
+      };
+      d.nfused[P] = (int)(sizeof v / sizeof v[0]);
+      for (int i = 0; i < d.nfused[P]; ++i) d.fused[P][i] = v[i];
+      if constexpr (P == 0 || P == 2) {
+        const FgbBatchVariant b[] = {
+            Tb2dBatchVariant<Prog, P, Stage0, 64, 32, 1>::describe(),
+            Tb2dBatchVariant<Prog, P, Stage0, 64, 32, 2>::describe(),
+            Tb2dBatchVariant<Prog, P, Stage0, 64, 32, 4>::describe(),
+            Tb2dBatchVariant<Prog, P, Stage0, 64, 32, 8>::describe(),
+            Tb2dBatchVariant<Prog, P, Stage0, 32, 32, 4>::describe(),
+            Tb2dBatchVariant<Prog, P, Stage0, 128, 32, 4>::describe(),
+        };
+        d.nbatch[P] = (int)(sizeof b / sizeof b[0]);
+        for (int i = 0; i < d.nbatch[P]; ++i) d.batch[P][i] = b[i];
+      } else {
+        d.nbatch[P] = 0;
+      }
+    } else {
+      d.nfused[P] = 0;
+      d.nbatch[P] = 0;
+    }
+  }
+};
+
+template <class Adj>
+struct AdjointFill {
+  static void fill(FgbProgramDesc& d) {
+    if constexpr (std::is_same<Adj, void>::value) {
+      for (int p = 0; p < FGB_NUM_PRECISIONS; ++p) d.adjoint[p] = nullptr;
+    } else {
+      d.adjoint[0] = &launch_adjoint<0, Adj>;
+      d.adjoint[1] = &launch_adjoint<1, Adj>;
+      d.adjoint[2] = &launch_adjoint<2, Adj>;
+      d.adjoint[3] = nullptr;   // FP16 storage has no adjoint
+    }
+  }
+};
 
 template <class Prog, class... Stages>
 struct ProgramBuilder {
@@ -211,6 +324,11 @@ struct ProgramBuilder {
     fill<1>(d);
     fill<2>(d);
     fill<3>(d);
+    FusedFill<Prog, Stages...>::template fill<0>(d);
+    FusedFill<Prog, Stages...>::template fill<1>(d);
+    FusedFill<Prog, Stages...>::template fill<2>(d);
+    FusedFill<Prog, Stages...>::template fill<3>(d);
+    AdjointFill<typename Prog::Adjoint>::fill(d);
     return d;
   }
 };

@@ -1,0 +1,264 @@
+"""Adjoint (reverse-mode derivative) of a single-stage step function, emitted
+as a stage functor for the kernel templates.
+
+The forward step writes ``out[f][p + shift] = F_f(u at p + d for the cursors
+d it reads)``.  Its transpose, applied to an adjoint state ``lam`` (the
+derivative of a scalar loss with respect to ``out``), is
+
+    lam_in[g][q] = sum over f and cursors d of field g:
+                   lam[f][q - d + shift] * dF_f/du_g[d]  evaluated at p = q - d.
+
+The partial derivatives come from reverse-mode differentiation of the
+program's own SSA chain (seed 1 at each store).  Terms that do not depend
+on the grid are carried symbolically and folded on the host into the
+uniform table, so a linear stencil (heat) costs one multiply-add per cursor;
+terms that do (the reaction terms of Gray-Scott) are evaluated at ``q - d``
+from the forward state.  The reference has no adjoint (SURVEY 8(b) lists
+``Formura_Backward`` as an extension); the checkpointed gradient of the
+runtime (``fgb_gradient_*``) calls this step.
+"""
+from __future__ import annotations
+
+from typing import Dict, List, Tuple
+
+from .cuda import _ProgramEmitter, _StageEmitter, c_double
+from .manifest import MMProgram
+from .translate import FormuraCompileError
+
+_CMP = {"<", ">", "<=", ">=", "==", "!=", "&&", "||"}
+
+
+def _simplify(t):
+    k = t[0]
+    if k in ("lit", "node", "recip"):
+        return t
+    if k == "neg":
+        a = _simplify(t[1])
+        if a[0] == "lit":
+            return ("lit", -a[1])
+        return ("neg", a)
+    a, b = _simplify(t[1]), _simplify(t[2])
+    if a[0] == "lit" and b[0] == "lit":
+        return ("lit", {"+": a[1] + b[1], "-": a[1] - b[1], "*": a[1] * b[1], "/": a[1] / b[1]}[k])
+    if k == "*":
+        if a == ("lit", 1.0):
+            return b
+        if b == ("lit", 1.0):
+            return a
+    if k == "/" and b == ("lit", 1.0):
+        return a
+    return (k, a, b)
+
+
+class _OffsetEmitter(_StageEmitter):
+    """Forward values of the step at cursor offset ``e`` from the thread's cell."""
+
+    def __init__(self, prog, stage, shared_lines, memo, counter):
+        super().__init__(prog, stage)
+        self.lines = shared_lines
+        self.memo = memo
+        self._counter = counter
+        self.offset = (0, 0, 0)
+
+    def fresh(self) -> str:
+        self._counter[0] += 1
+        return f"t{self._counter[0]}"
+
+    def micro(self, mn, micro, node):
+        inst = mn.inst
+        if inst[0] == "loadstatic":
+            c = self.p.cursor3(inst[1])
+            c = [a + b for a, b in zip(c, self.offset)]
+            f = self.p.fields.index(inst[2])
+            return self.bind(f"a.template ld<{f}, {c[0]}, {c[1]}, {c[2]}>()")
+        if inst[0] == "store":
+            return None
+        return super().micro(mn, micro, node)
+
+
+class _Algebra:
+    """Values of the reverse sweep: ('u', tree) grid-independent, or an
+    emitted handle of the offset emitter."""
+
+    def __init__(self, fe: _OffsetEmitter, pe: _ProgramEmitter):
+        self.fe, self.pe = fe, pe
+
+    def T(self, v) -> str:
+        if v[0] == "u":
+            t = _simplify(v[1])
+            if t[0] == "lit":
+                return f"T({c_double(t[1])})"
+            return f"U[{self.pe.table_index(('expr', t))}]"
+        return self.fe.as_T(v)
+
+    def binop(self, k, a, b, fn):
+        if a[0] == "u" and b[0] == "u":
+            return ("u", _simplify((k, a[1], b[1])))
+        if k == "*":
+            for x, y in ((a, b), (b, a)):
+                if x == ("u", ("lit", 1.0)):
+                    return y
+        if k == "/" and b[0] == "u":
+            return self.fe.bind(f"M::mul({self.T(a)}, {self.T(('u', ('/', ('lit', 1.0), b[1])))})")
+        return self.fe.bind(f"M::{fn}({self.T(a)}, {self.T(b)})")
+
+    def add(self, a, b):
+        return self.binop("+", a, b, "add")
+
+    def sub(self, a, b):
+        return self.binop("-", a, b, "sub")
+
+    def mul(self, a, b):
+        return self.binop("*", a, b, "mul")
+
+    def div(self, a, b):
+        return self.binop("/", a, b, "div")
+
+    def neg(self, a):
+        if a[0] == "u":
+            return ("u", _simplify(("neg", a[1])))
+        return self.fe.bind(f"M::neg({self.T(a)})")
+
+
+def emit_adjoint(mm: MMProgram, name: str, pe: _ProgramEmitter = None):
+    """(CUDA source of ``struct Adjoint``, program emitter holding its table).
+    Pass the forward program's emitter so that both share one uniform table."""
+    pe = pe or _ProgramEmitter(mm, name, [])
+    if len(pe.stages) != 1 or pe.mids:
+        raise FormuraCompileError("the generated adjoint covers single-stage programs")
+    stage = pe.stages[0]
+    fields = pe.fields
+    shift = pe.shift
+    an = pe.an
+    lines: List[str] = []
+    memo: Dict[tuple, tuple] = {}
+    counter = [0]
+    offsets = set()
+    for node in stage.nodes:
+        for mn in node.micro:
+            if mn.inst[0] == "loadstatic":
+                offsets.add(tuple(-x for x in pe.cursor3(mn.inst[1])))
+    acc: Dict[int, List[str]] = {g: [] for g in range(len(fields))}
+
+    for e in sorted(offsets):
+        fe = _OffsetEmitter(pe, stage, lines, memo, counter)
+        fe.offset = e
+        alg = _Algebra(fe, pe)
+        for node in stage.nodes:
+            if not node.is_store:
+                raise FormuraCompileError("single-stage programs store every manifest value")
+            micro = node.micro
+            fwd: Dict[int, tuple] = {}
+
+            def value(i):
+                """Forward value of micro node i at this offset (lazy)."""
+                if i in fwd:
+                    return fwd[i]
+                mn = micro[i]
+                if mn.inst[0] != "loadstatic" and an.om_uniform(mn.key[1]):
+                    omid = mn.key[1]
+                    v = ("u", ("node", omid)) if an.om_config_dependent(omid) else \
+                        ("u", ("lit", float(an.om_value(omid))))
+                else:
+                    for j in range(i + 1):
+                        if micro[j].key not in fe.var:
+                            h = fe.micro(micro[j], micro, node)
+                            if h is not None:
+                                fe.var[micro[j].key] = h
+                    v = fe.var[mn.key]
+                fwd[i] = v
+                return v
+
+            fe.var = {}
+            store = micro[-1]
+            f = fields.index(store.inst[1])
+            bar: Dict[int, List[tuple]] = {store.inst[2]: [("u", ("lit", 1.0))]}
+            for i in range(len(micro) - 2, -1, -1):
+                if i not in bar:
+                    continue
+                mn = micro[i]
+                inst = mn.inst
+                k = inst[0]
+                total = bar[i][0]
+                for t in bar[i][1:]:
+                    total = alg.add(total, t)
+                bar[i] = [total]
+                if k in ("imm", "loadindex", "loadcursor", "loadstatic"):
+                    continue
+                if an.om_uniform(mn.key[1]):
+                    continue
+                Y = total
+
+                def push(j, v):
+                    # v is a thunk: derivative terms are built only for operands
+                    # that depend on the grid
+                    if micro[j].inst[0] == "loadstatic" or not an.om_uniform(micro[j].key[1]):
+                        bar.setdefault(j, []).append(v())
+
+                if k == "uniop":
+                    op, a = inst[1], inst[2]
+                    if op == "+":
+                        push(a, lambda: Y)
+                    elif op == "-":
+                        push(a, lambda: alg.neg(Y))
+                    else:
+                        fn = op[len("external-call/"):]
+                        x = alg.T(value(a))
+                        y = alg.T(value(i))
+                        d = {"sqrt": f"M::div(T(0.5), {y})", "exp": y, "log": f"M::div(T(1), {x})",
+                             "sin": f"M::cos({x})", "cos": f"M::neg(M::sin({x}))",
+                             "fabs": f"({x} < T(0) ? T(-1) : T(1))"}.get(fn)
+                        if d is None:
+                            raise FormuraCompileError(f"no derivative for {fn}")
+                        push(a, lambda: alg.mul(Y, fe.bind(d)))
+                elif k == "binop":
+                    op, a, b = inst[1], inst[2], inst[3]
+                    if op in _CMP:
+                        continue
+                    if op == "+":
+                        push(a, lambda: Y)
+                        push(b, lambda: Y)
+                    elif op == "-":
+                        push(a, lambda: Y)
+                        push(b, lambda: alg.neg(Y))
+                    elif op == "*":
+                        push(a, lambda: alg.mul(Y, value(b)))
+                        push(b, lambda: alg.mul(Y, value(a)))
+                    elif op == "/":
+                        push(a, lambda: alg.div(Y, value(b)))
+                        if not an.om_uniform(micro[b].key[1]):
+                            push(b, lambda: alg.neg(alg.div(alg.mul(Y, value(i)), value(b))))
+                    elif op == "**":
+                        A, B = alg.T(value(a)), alg.T(value(b))
+                        push(a, lambda: alg.mul(Y, fe.bind(f"M::mul({B}, M::pow({A}, M::sub({B}, T(1))))")))
+                        if not an.om_uniform(micro[b].key[1]):
+                            push(b, lambda: alg.mul(Y, fe.bind(f"M::mul({alg.T(value(i))}, M::log({A}))")))
+                    else:
+                        raise FormuraCompileError(f"no derivative for {op}")
+                elif k == "triop":
+                    c, a, b = inst[2], inst[3], inst[4]
+                    C = fe.as_bool(value(c))
+                    push(a, lambda: fe.bind(f"({C} ? {alg.T(Y)} : T(0))"))
+                    push(b, lambda: fe.bind(f"({C} ? T(0) : {alg.T(Y)})"))
+            s3 = [x + shift if i >= 3 - pe.dim else x for i, x in enumerate(e)]
+            lam = None
+            for i, mn in enumerate(micro):
+                if mn.inst[0] == "loadstatic" and i in bar:
+                    c = tuple(pe.cursor3(mn.inst[1]))
+                    if tuple(-x for x in c) == e:
+                        if lam is None:
+                            lam = fe.bind(f"a.template ldl<{f}, {s3[0]}, {s3[1]}, {s3[2]}>()")
+                        g = fields.index(mn.inst[2])
+                        acc[g].append(alg.T(alg.mul(lam, bar[i][0])))
+    out = []
+    for g in range(len(fields)):
+        terms = acc[g]
+        expr = terms[0] if terms else "T(0)"
+        for t in terms[1:]:
+            expr = f"M::add({expr}, {t})"
+        out.append(f"    a.template stl<{g}>({expr});")
+    body = "\n".join("    " + l.strip() for l in lines) + "\n" + "\n".join(out)
+    return (f"struct Adjoint {{\n"
+            f"  template <class M, class A>\n"
+            f"  static __device__ __forceinline__ void run(const A& a, const typename M::T* __restrict__ U) {{\n"
+            f"    using T = typename M::T;\n    (void)U;\n{body}\n  }}\n}};\n"), pe

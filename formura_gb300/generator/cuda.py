@@ -311,6 +311,7 @@ class _StageEmitter:
         self.stage = stage
         self.lines: List[str] = []
         self.var: Dict[tuple, object] = {}     # key -> expression handle
+        self.memo: Dict[tuple, tuple] = {}     # (expression, type) -> handle
         self.n = 0
 
     def fresh(self) -> str:
@@ -384,16 +385,12 @@ class _StageEmitter:
         if k == "loadstatic":
             c = self.p.cursor3(inst[1])
             f = self.p.fields.index(inst[2])
-            name = self.fresh()
-            self.emit(f"const T {name} = a.template ld<{f}, {c[0]}, {c[1]}, {c[2]}>();")
-            return ("v", name, "T")
+            return self.bind(f"a.template ld<{f}, {c[0]}, {c[1]}, {c[2]}>()")
         if k == "loadcursor":
             dep = inst[2]
             c = self.p.cursor3(inst[1])
             kk = self.p.mids.index(dep)
-            name = self.fresh()
-            self.emit(f"const T {name} = a.template ldm<{kk}, {c[0]}, {c[1]}, {c[2]}>();")
-            return ("v", name, "T")
+            return self.bind(f"a.template ldm<{kk}, {c[0]}, {c[1]}, {c[2]}>()")
         if k == "loadindex":
             raise FormuraCompileError("index variables inside the step function are not supported "
                                       "by the GPU backend")
@@ -468,9 +465,16 @@ class _StageEmitter:
         return f"({self.as_T(h)} != T(0))"
 
     def bind(self, expr: str, ctype: str = "T"):
+        # value numbering: the same operation on the same operands is the same
+        # value (every operation is deterministic), so it is computed once
+        hit = self.memo.get((expr, ctype))
+        if hit is not None:
+            return hit
         name = self.fresh()
         self.emit(f"const {ctype} {name} = {expr};")
-        return ("v", name, ctype)
+        h = ("v", name, ctype)
+        self.memo[(expr, ctype)] = h
+        return h
 
 
 class _ProgramEmitter:
@@ -533,7 +537,17 @@ class _ProgramEmitter:
                 f"  static __device__ __forceinline__ void run(const A& a, const typename M::T* __restrict__ U) {{\n"
                 f"    using T = typename M::T;\n"
                 f"    (void)U;\n{body}\n  }}\n}};\n")
+        adj_src = None
+        if len(self.stages) == 1 and not self.mids:
+            from .adjoint import emit_adjoint
+            try:
+                adj_src, _ = emit_adjoint(self.mm, self.name, self)
+            except FormuraCompileError:
+                adj_src = None
+        if adj_src:
+            out.append(adj_src)
         out.append(f"struct Prog {{\n"
+                   f"  using Adjoint = {'Adjoint' if adj_src else 'void'};\n"
                    f"  static constexpr int kDim = {self.dim};\n"
                    f"  static constexpr int kFields = {len(self.fields)};\n"
                    f"  static constexpr int kMids = {len(self.mids)};\n"
@@ -558,11 +572,35 @@ def emit_cuda(mm: MMProgram, name: str, runtime_params: Optional[List[str]] = No
     return _ProgramEmitter(mm, name, runtime_params or []).emit()
 
 
+def eval_utree(an: "_Analysis", tree, params=None) -> float:
+    """Host value of a grid-independent expression tree: ('lit', x),
+    ('node', omid), ('recip', omid) or (op, a[, b]) with op in + - * / neg."""
+    k = tree[0]
+    if k == "lit":
+        return float(tree[1])
+    if k == "node":
+        return float(an.om_value(tree[1], params))
+    if k == "recip":
+        return 1.0 / float(an.om_value(tree[1], params))
+    if k == "neg":
+        return -eval_utree(an, tree[1], params)
+    a = eval_utree(an, tree[1], params)
+    b = eval_utree(an, tree[2], params)
+    return {"+": a + b, "-": a - b, "*": a * b, "/": a / b}[k]
+
+
 def uniform_table(mm: MMProgram, kp: KernelProgram, params: Optional[Dict[str, float]] = None) -> List[float]:
     """Host values of the runtime uniform table for one configuration."""
     an = _Analysis(mm, kp.runtime_params)
     out = []
-    for kind, omid in kp.uniform_exprs:
-        v = an.om_value(omid, params)
-        out.append(float(v) if kind == "node" else 1.0 / float(v))
+    for entry in kp.uniform_exprs:
+        kind = entry[0]
+        if kind == "node":
+            out.append(float(an.om_value(entry[1], params)))
+        elif kind == "recip":
+            out.append(1.0 / float(an.om_value(entry[1], params)))
+        elif kind == "expr":
+            out.append(eval_utree(an, entry[1], params))
+        else:
+            raise FormuraCompileError(f"unknown uniform table entry {kind}")
     return out

@@ -15,7 +15,9 @@ Backend options come from ``gpu_*`` keys of the numerical config:
 ``gpu_precision`` (f64, f64fast, f32, f16), ``gpu_steps_per_forward``
 (default: ``temporal_blocking_interval`` when temporal blocking is
 configured, else 1, i.e. the reference's step count per call) and
-``gpu_field_scales`` (FP16 storage).
+``gpu_field_scales`` (FP16 storage) and ``gpu_autotune`` (0 turns off the
+choice of the temporal-blocking kernel at ``Formura_Init``; results do not
+depend on it except with FP16 storage).
 """
 from __future__ import annotations
 
@@ -176,6 +178,9 @@ def emit_dropin(mm: MMProgram, program: str, header_name: str,
             raise FormuraCompileError("gpu_field_scales needs one scale per field")
         c.append(f"static const float scales[{len(fields)}] = {{" + ", ".join(f"{float(x)!r}f" for x in sc) + "};")
         c.append(f'formura_gb300_check(fgb_set_scales(formura_gb300_grid, scales, {len(fields)}), "fgb_set_scales");')
+    tune = cfg.gpu.get("gpu_autotune", 1)
+    if int(tune):
+        c.append(f'formura_gb300_check(fgb_autotune(formura_gb300_grid, {max(8, 2 * nt) if nt < 64 else 64}, 0), "fgb_autotune");')
     c.append(f"fgb_host_register(&{gsn}, sizeof({gsn}));")
     c.append("}")
     c.append("void Formura_Forward(Formura_Navi *n) {")

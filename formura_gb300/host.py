@@ -65,6 +65,17 @@ class Library:
         L.fgb_launch_count.argtypes = [ctypes.c_void_p]
         L.fgb_launch_count.restype = ctypes.c_int64
         L.fgb_set_scales.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_float), ctypes.c_int]
+        L.fgb_variant_count.argtypes = [ctypes.c_void_p]
+        L.fgb_variant_info.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 3
+        L.fgb_set_variant.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.fgb_variant.argtypes = [ctypes.c_void_p]
+        L.fgb_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        L.fgb_backward.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.fgb_gradient_forward.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_int]
+        L.fgb_gradient_backward.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.fgb_gradient_backward_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
+        L.fgb_gradient_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
+        L.fgb_adjoint_steps.argtypes = [ctypes.c_void_p, ctypes.c_int]
 
     @classmethod
     def get(cls) -> "Library":
@@ -135,6 +146,59 @@ class Grid:
     def synchronize(self):
         self.L.check(self.L.lib.fgb_synchronize(self.h), "fgb_synchronize")
 
+    def variants(self) -> List[Dict[str, int]]:
+        out = []
+        for i in range(self.L.lib.fgb_variant_count(self.h)):
+            v = [ctypes.c_int() for _ in range(3)]
+            self.L.check(self.L.lib.fgb_variant_info(self.h, i, *[ctypes.byref(x) for x in v]), "variant_info")
+            out.append({"index": i, "tile_x": v[0].value, "tile_y": v[1].value, "steps": v[2].value})
+        return out
+
+    def set_variant(self, index: int):
+        self.L.check(self.L.lib.fgb_set_variant(self.h, int(index)), "fgb_set_variant")
+
+    @property
+    def variant(self) -> int:
+        return self.L.lib.fgb_variant(self.h)
+
+    def autotune(self, trial_steps: int = 32) -> int:
+        c = ctypes.c_int()
+        self.L.check(self.L.lib.fgb_autotune(self.h, int(trial_steps), ctypes.byref(c)), "fgb_autotune")
+        return c.value
+
+    # -- reverse mode -----------------------------------------------------
+    def backward(self, lam_next: np.ndarray) -> np.ndarray:
+        """One adjoint step at the current state: (dF/du)^T lam_next."""
+        a = np.ascontiguousarray(lam_next, dtype=np.float64)
+        out = np.empty((self.nfields,) + self.shape, np.float64)
+        self.L.check(self.L.lib.fgb_backward(self.h, a.ctypes.data, out.ctypes.data), "fgb_backward")
+        return out
+
+    def adjoint_steps(self, nsteps: int):
+        self.L.check(self.L.lib.fgb_adjoint_steps(self.h, int(nsteps)), "fgb_adjoint_steps")
+
+    def gradient_forward(self, nsteps: int, snapshots: int):
+        self.L.check(self.L.lib.fgb_gradient_forward(self.h, int(nsteps), int(snapshots)), "fgb_gradient_forward")
+
+    def gradient_backward(self, seed: np.ndarray) -> np.ndarray:
+        a = np.ascontiguousarray(seed, dtype=np.float64)
+        out = np.empty((self.nfields,) + self.shape, np.float64)
+        self.L.check(self.L.lib.fgb_gradient_backward(self.h, a.ctypes.data, out.ctypes.data),
+                     "fgb_gradient_backward")
+        return out
+
+    def gradient_stats(self):
+        f, a = ctypes.c_int64(), ctypes.c_int64()
+        self.L.check(self.L.lib.fgb_gradient_stats(self.h, ctypes.byref(f), ctypes.byref(a)), "fgb_gradient_stats")
+        return {"forward_steps": f.value, "adjoint_steps": a.value}
+
+    def gradient(self, u0: np.ndarray, nsteps: int, snapshots: int, seed_fn):
+        """(u_T, dJ/du_0) for a loss J(u_T) whose derivative seed_fn(u_T) gives."""
+        self.upload(u0)
+        self.gradient_forward(nsteps, snapshots)
+        uT = self.download()
+        return uT, self.gradient_backward(seed_fn(uT))
+
     @property
     def stream(self) -> int:
         return self.L.lib.fgb_stream(self.h)
@@ -149,10 +213,100 @@ class Grid:
         return [int(x) for x in p]
 
 
+class Batch:
+    """An ensemble of independent 2D grids of one program (fgb_batch_*)."""
+
+    def __init__(self, program: str, shapes: Sequence[Sequence[int]], precision: str,
+                 uniforms: Sequence[Sequence[float]], lib: Optional[Library] = None):
+        self.L = lib or Library.get()
+        L = self.L.lib
+        L.fgb_batch_open.argtypes = [ctypes.c_char_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int), ctypes.c_int,
+                                     ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.POINTER(ctypes.c_void_p)]
+        for fn in ("fgb_batch_close", "fgb_batch_synchronize", "fgb_batch_variant_count", "fgb_batch_variant"):
+            getattr(L, fn).argtypes = [ctypes.c_void_p]
+        L.fgb_batch_upload.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.fgb_batch_download.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
+        L.fgb_batch_forward.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.fgb_batch_set_variant.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.fgb_batch_variant_info.argtypes = [ctypes.c_void_p, ctypes.c_int] + [ctypes.POINTER(ctypes.c_int)] * 3
+        L.fgb_batch_autotune.argtypes = [ctypes.c_void_p, ctypes.c_int, ctypes.POINTER(ctypes.c_int)]
+        L.fgb_batch_stream.argtypes = [ctypes.c_void_p]
+        L.fgb_batch_stream.restype = ctypes.c_void_p
+        L.fgb_batch_launch_count.argtypes = [ctypes.c_void_p]
+        L.fgb_batch_launch_count.restype = ctypes.c_int64
+        self.shapes = [tuple(int(x) for x in sh) for sh in shapes]
+        self.nfields = self.L.query(program)["nfields"]
+        nu = len(uniforms[0]) if len(uniforms) else 0
+        flat = [float(x) for u in uniforms for x in u]
+        shp = (ctypes.c_int * (2 * len(self.shapes)))(*[x for sh in self.shapes for x in sh])
+        u = (ctypes.c_double * max(1, len(flat)))(*flat)
+        h = ctypes.c_void_p()
+        self.L.check(L.fgb_batch_open(program.encode(), len(self.shapes), shp, PRECISIONS[precision], u, nu,
+                                      ctypes.byref(h)), "fgb_batch_open")
+        self.h = h
+
+    def close(self):
+        if self.h:
+            self.L.lib.fgb_batch_close(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def upload(self, i: int, state: np.ndarray):
+        a = np.ascontiguousarray(state, dtype=np.float64)
+        self.L.check(self.L.lib.fgb_batch_upload(self.h, i, a.ctypes.data), "fgb_batch_upload")
+
+    def download(self, i: int) -> np.ndarray:
+        out = np.empty((self.nfields,) + self.shapes[i], np.float64)
+        self.L.check(self.L.lib.fgb_batch_download(self.h, i, out.ctypes.data), "fgb_batch_download")
+        return out
+
+    def forward(self, nsteps: int):
+        self.L.check(self.L.lib.fgb_batch_forward(self.h, int(nsteps)), "fgb_batch_forward")
+
+    def synchronize(self):
+        self.L.check(self.L.lib.fgb_batch_synchronize(self.h), "fgb_batch_synchronize")
+
+    def variants(self):
+        out = []
+        for i in range(self.L.lib.fgb_batch_variant_count(self.h)):
+            v = [ctypes.c_int() for _ in range(3)]
+            self.L.check(self.L.lib.fgb_batch_variant_info(self.h, i, *[ctypes.byref(x) for x in v]), "info")
+            out.append({"index": i, "tile_x": v[0].value, "tile_y": v[1].value, "steps": v[2].value})
+        return out
+
+    def set_variant(self, i: int):
+        self.L.check(self.L.lib.fgb_batch_set_variant(self.h, int(i)), "fgb_batch_set_variant")
+
+    @property
+    def variant(self) -> int:
+        return self.L.lib.fgb_batch_variant(self.h)
+
+    def autotune(self, trial_steps: int = 32) -> int:
+        c = ctypes.c_int()
+        self.L.check(self.L.lib.fgb_batch_autotune(self.h, int(trial_steps), ctypes.byref(c)), "fgb_batch_autotune")
+        return c.value
+
+    @property
+    def stream(self) -> int:
+        return self.L.lib.fgb_batch_stream(self.h)
+
+    @property
+    def launches(self) -> int:
+        return self.L.lib.fgb_batch_launch_count(self.h)
+
+
 def program_uniforms(fmr_src: str, yaml_text: str, program: str,
-                     params: Optional[Dict[str, float]] = None, runtime_params: Sequence[str] = ()):
-    """(compiled MM program, uniform table) of a program for one config."""
+                     params: Optional[Dict[str, float]] = None, runtime_params: Optional[Sequence[str]] = None):
+    """(compiled MM program, uniform table) of a library program for one
+    config; `params` overrides the runtime parameters (e.g. F, kappa)."""
     mm = compile_program(fmr_src, decode_config(yaml_text))
+    if runtime_params is None:
+        runtime_params = _build.library_runtime_params(program)
     kp = emit_cuda(mm, program, list(runtime_params))
     return mm, uniform_table(mm, kp, params)
 
@@ -166,11 +320,13 @@ class FormuraProgram:
     """The generated C API of one program, running on the GB300 backend."""
 
     def __init__(self, fmr_src: str, yaml_text: str, program: str, name: Optional[str] = None,
-                 params: Optional[Dict[str, float]] = None, runtime_params: Sequence[str] = (),
+                 params: Optional[Dict[str, float]] = None, runtime_params: Optional[Sequence[str]] = None,
                  build_dir: Optional[str] = None):
         lib = Library.get()
         self.mm = compile_program(fmr_src, decode_config(yaml_text))
         name = name or program
+        if runtime_params is None:
+            runtime_params = _build.library_runtime_params(program)
         h, c = emit_dropin(self.mm, program, f"{name}.h", params, list(runtime_params))
         key = hashlib.sha1((h + c + lib.path).encode()).hexdigest()[:12]
         d = os.path.join(build_dir or os.path.join(_build.BUILD, "dropin"), f"{name}_{key}")

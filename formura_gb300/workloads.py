@@ -84,3 +84,45 @@ def hllc_state(shape: Tuple[int, int, int], seed: int = 0, gamma: float = 1.4,
     p = np.ones(shape)
     e = p / (gamma - 1.0) + 0.5 * rho * (v[0] ** 2 + v[1] ** 2 + v[2] ** 2)
     return {"rho": rho, "mx": rho * v[0], "my": rho * v[1], "mz": rho * v[2], "e": e}
+
+
+def gaussians_3d(shape: Tuple[int, int, int], seed: int, count: int = 32,
+                 wmin: float = 4.0, wmax: float = 16.0) -> np.ndarray:
+    """Smooth periodic field: a sum of `count` Gaussians with random centres,
+    widths uniform in [wmin, wmax] cells and amplitudes N(0, 1)."""
+    rng = np.random.default_rng(seed)
+    idx = [np.arange(n, dtype=np.float64) for n in shape]
+    out = np.zeros(shape)
+    for _ in range(count):
+        c = [rng.uniform(0, n) for n in shape]
+        w = rng.uniform(wmin, wmax)
+        amp = rng.normal()
+        g = 1.0
+        parts = []
+        for ax, n in enumerate(shape):
+            d = np.abs(idx[ax] - c[ax])
+            d = np.minimum(d, n - d)                 # periodic distance
+            parts.append(np.exp(-0.5 * (d / w) ** 2))
+        out += amp * parts[0][:, None, None] * parts[1][None, :, None] * parts[2][None, None, :]
+    return out
+
+
+def ensemble(count: int = 256, seed: int = 0, nmin: int = 64, nmax: int = 1024):
+    """Gray-Scott ensemble: side lengths log-uniform in [nmin, nmax], feed
+    rate F ~ U[0.02, 0.06] and kill rate k ~ U[0.05, 0.065] per grid."""
+    rng = np.random.default_rng(seed)
+    sides = np.rint(np.exp(rng.uniform(np.log(nmin), np.log(nmax), count))).astype(int)
+    F = rng.uniform(0.02, 0.06, count)
+    k = rng.uniform(0.05, 0.065, count)
+    return [(int(n), float(f), float(kk)) for n, f, kk in zip(sides, F, k)]
+
+
+def gs_square_state(n: int, seed: int) -> np.ndarray:
+    """Gray-Scott initial state of an n x n grid: u = 1, v = 0 outside and
+    u = 0.5, v = 0.25 inside the centred 10% square, plus uniform noise in
+    [-0.01, 0.01] on both fields."""
+    i = np.arange(n)
+    inside = (i > 0.45 * n) & (i < 0.55 * n)
+    sq = inside[:, None] & inside[None, :]
+    st = gs_perturb(np.where(sq, 0.5, 1.0), np.where(sq, 0.25, 0.0), seed)
+    return np.stack([st["u"], st["v"]])

@@ -82,6 +82,70 @@ int fgb_state_device(fgb_grid* grid, void** field_ptrs, int nfields);
 /* Number of kernels this grid has launched so far. */
 int64_t fgb_launch_count(fgb_grid* grid);
 
+/* Temporal-blocking kernels.  Programs whose step is a single stage also
+ * have kernels that advance several steps per launch in shared-memory tiles
+ * (they replace the reference's CPU temporal blocking, Templates.hs:311-381).
+ * fgb_autotune times every variant that fits on this device and the
+ * one-step kernel over `trial_steps` steps, restores the state, and selects
+ * the fastest; fgb_set_variant selects one by index (-1: one step per
+ * launch).  FP64 and FP32 results do not depend on the choice; with FP16
+ * storage the tiles keep FP32 values between the steps of one launch. */
+int fgb_variant_count(fgb_grid* grid);
+int fgb_variant_info(fgb_grid* grid, int index, int* tile_x, int* tile_y, int* steps);
+int fgb_set_variant(fgb_grid* grid, int index);
+int fgb_variant(fgb_grid* grid);
+int fgb_autotune(fgb_grid* grid, int trial_steps, int* chosen);
+
+/* Reverse mode (no counterpart in the reference; SURVEY 8(b) names
+ * Formura_Backward as the extension).  The adjoint step is generated from
+ * the program's own step function by reverse-mode differentiation
+ * (single-stage programs, FP64 and FP32).
+ *
+ * fgb_backward: one adjoint step at the current state u_n:
+ *   lambda = (dF/du at u_n)^T lambda_next   (host FP64, formura_data layout).
+ * fgb_gradient_forward / fgb_gradient_backward: gradient of a scalar loss of
+ * the state `nsteps` steps ahead with respect to the current state.  The
+ * forward call checkpoints the current state u_0 and advances to u_T; the
+ * caller computes seed = dJ/du_T; the backward call returns dJ/du_0 and
+ * leaves the state at u_0.  `snapshots` device checkpoints (u_0 included)
+ * bound the memory; the reversal places them by the binomial rule of
+ * Griewank's revolve and recomputes forward segments in between.
+ * fgb_gradient_stats: forward steps (including recomputation) and adjoint
+ * steps of the last gradient. */
+int fgb_backward(fgb_grid* grid, const double* lambda_next, double* lambda);
+int fgb_gradient_forward(fgb_grid* grid, int nsteps, int snapshots);
+int fgb_gradient_backward(fgb_grid* grid, const double* seed, double* grad);
+int fgb_gradient_backward_device(fgb_grid* grid, const void* seed, void* grad);
+int fgb_gradient_stats(fgb_grid* grid, int64_t* forward_steps, int64_t* adjoint_steps);
+/* Apply the adjoint step `nsteps` times to the device adjoint state at the
+ * current forward state (enqueued; for linear steps and for timing). */
+int fgb_adjoint_steps(fgb_grid* grid, int nsteps);
+
+/* Batched ensembles (no counterpart in the reference, which runs one grid
+ * per process): `count` independent periodic 2D grids of one single-stage
+ * program, grid i of extent shapes[2i] x shapes[2i+1] with its own uniform
+ * table uniforms[i*nuniforms ...] (e.g. per-grid feed and kill rates).  All
+ * grids advance together: persistent CTAs walk one tile queue spanning every
+ * grid, several steps per launch in shared memory; fgb_batch_forward replays
+ * a CUDA graph of 64 steps for long runs; fgb_batch_autotune picks the tile
+ * shape and steps per launch.  FP64 and FP32 only.  Each grid's result is
+ * bit-identical to running it alone with fgb_open / fgb_forward. */
+typedef struct fgb_batch fgb_batch;
+int fgb_batch_open(const char* program, int count, const int* shapes, int precision,
+                   const double* uniforms, int nuniforms, fgb_batch** out);
+int fgb_batch_close(fgb_batch* batch);
+int fgb_batch_upload(fgb_batch* batch, int index, const double* host_state);
+int fgb_batch_download(fgb_batch* batch, int index, double* host_state);
+int fgb_batch_forward(fgb_batch* batch, int nsteps);
+int fgb_batch_synchronize(fgb_batch* batch);
+int fgb_batch_variant_count(fgb_batch* batch);
+int fgb_batch_variant_info(fgb_batch* batch, int index, int* tile_x, int* tile_y, int* steps);
+int fgb_batch_set_variant(fgb_batch* batch, int index);
+int fgb_batch_variant(fgb_batch* batch);
+int fgb_batch_autotune(fgb_batch* batch, int trial_steps, int* chosen);
+void* fgb_batch_stream(fgb_batch* batch);
+int64_t fgb_batch_launch_count(fgb_batch* batch);
+
 /* Pin a host range (e.g. formura_data) for faster copies; optional. */
 int fgb_host_register(void* ptr, size_t bytes);
 int fgb_host_unregister(void* ptr);

@@ -1,0 +1,76 @@
+"""Temporal-blocking kernels (several steps per launch in shared-memory
+tiles): every variant gives the same state as one step per launch, bit for
+bit in FP64 and FP32, including grids that are not multiples of the tile and
+step counts that are not multiples of the fused depth."""
+import numpy as np
+import pytest
+
+from formura_gb300 import workloads as W
+from formura_gb300.host import Grid, builtin_program, program_uniforms
+
+pytestmark = pytest.mark.gpu
+
+
+def _state(shape, seed):
+    st = W.gs_perturb(np.ones(shape), np.zeros(shape), seed)
+    u, v = st["u"], st["v"]
+    # a square of active pattern so both fields vary
+    c = tuple(slice(s // 3, 2 * s // 3) for s in shape)
+    u[c] = 0.5 + 0.01 * np.random.default_rng(seed).random(u[c].shape)
+    v[c] = 0.25
+    return np.stack([u, v])
+
+
+@pytest.mark.parametrize("shape", [(256, 256), (100, 70), (64, 200)])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_every_variant_matches_single_steps(shape, prec):
+    src, _ = builtin_program("gs2d")
+    _, U = program_uniforms(src, W.gs_config(shape[0]), "gs2d")
+    x = _state(shape, 1)
+    steps = 37
+    g = Grid("gs2d", shape, prec, U)
+    g.upload(x)
+    g.forward(steps)
+    ref = g.download()
+    assert len(g.variants()) >= 4
+    for v in g.variants():
+        g.upload(x)
+        try:
+            g.set_variant(v["index"])
+        except Exception:
+            continue            # does not fit this device's shared memory
+        g.forward(steps)
+        got = g.download()
+        assert np.array_equal(got, ref), v
+    g.close()
+
+
+def test_autotune_preserves_state_and_picks_a_variant():
+    shape = (512, 512)
+    src, _ = builtin_program("gs2d")
+    _, U = program_uniforms(src, W.gs_config(shape[0]), "gs2d")
+    x = _state(shape, 2)
+    g = Grid("gs2d", shape, "f32", U)
+    g.upload(x)
+    before = g.download()
+    chosen = g.autotune(32)
+    assert chosen >= -1 and g.variant == chosen
+    assert np.array_equal(g.download(), before)
+    g.close()
+
+
+def test_f16_fused_close_to_f32():
+    shape = (256, 256)
+    src, _ = builtin_program("gs2d")
+    _, U = program_uniforms(src, W.gs_config(shape[0]), "gs2d")
+    x = _state(shape, 3)
+    a = Grid("gs2d", shape, "f32", U)
+    a.upload(x)
+    a.forward(64)
+    b = Grid("gs2d", shape, "f16", U, scales=[1.0, 0.5])
+    b.upload(x)
+    b.autotune(16)
+    b.forward(64)
+    fa, fb = a.download(), b.download()
+    for i in range(2):
+        assert W.rel_l2(fb[i], fa[i]) < 2e-2
