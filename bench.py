@@ -108,6 +108,11 @@ def workload_spec(name: str):
         return {"program": "hllc3d", "cfg": W.hllc_config(n), "shape": (n, n, n), "fields": 5,
                 "steps_total": 500, "cpu_cfg": W.hllc_config(128), "cpu_shape": (128, 128, 128),
                 "label": "hllc-euler-3d 256^3 periodic, gamma=1.4, MUSCL-minmod + HLLC, CFL 0.4, 500 steps"}
+    if name == "hlld3d":
+        n = 128
+        return {"program": "hlld3d", "cfg": W.mhd_config(n), "shape": (n, n, n), "fields": 9,
+                "steps_total": 100, "cpu_cfg": W.mhd_config(48), "cpu_shape": (48, 48, 48),
+                "label": "hlld-mhd-3d 128^3 periodic, gamma=5/3, MUSCL-minmod + HLLD + GLM, CFL 0.3"}
     raise SystemExit(f"unknown workload {name}")
 
 
@@ -120,6 +125,9 @@ def initial_state(spec, prog):
         return np.stack([st["u"], st["v"]])
     if spec["program"] == "hllc3d":
         st = W.hllc_state(tuple(prog.shape), seed=0)
+        return np.stack([st[f] for f in prog.fields])
+    if spec["program"] == "hlld3d":
+        st = W.mhd_state(tuple(prog.shape), seed=0)
         return np.stack([st[f] for f in prog.fields])
     return W.heat_state(spec["shape"], seed=0)["q"][None]
 
@@ -355,7 +363,7 @@ def main():
     ap.add_argument("--steps", type=int, default=None)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--workload", default="gs2d", choices=["gs2d", "heat3d", "hllc3d", "adjoint", "batch"])
+    ap.add_argument("--workload", default="gs2d", choices=["gs2d", "heat3d", "hllc3d", "hlld3d", "adjoint", "batch"])
     ap.add_argument("--precision", default="f64", choices=["f64", "f64fast", "f32", "f16"])
     ap.add_argument("--spf", type=int, default=100, help="time steps per bench step")
     ap.add_argument("--e2e-steps", type=int, default=20)
@@ -542,7 +550,10 @@ def run_batch(args):
         g.forward(steps)
         f64 = g.download()
         g.close()
-        errs.append(max(W.rel_l2(f32_final[i][j], f64[j]) for j in range(2)))
+        # error relative to the initial field's norm: where a pattern dies
+        # out, v decays towards 0 and a norm of the final field says nothing
+        errs.append(max(float(np.linalg.norm(f32_final[i][j] - f64[j]) / np.linalg.norm(X[i][j]))
+                        for j in range(2)))
     t64 = time.perf_counter() - t0
     v64 = cells * steps / t64 / 1e9
     line = {"metric": "GLUP/s", "value": value, "unit": "GLUP/s", "n_gpus": 1, "steps": 1,
@@ -556,7 +567,8 @@ def run_batch(args):
             "sequential_f64": {"value": v64, "unit": "GLUP/s", "seconds": t64,
                                "note": "256 sequential fgb_open/forward/download runs, bit-faithful FP64"},
             "speedup_vs_sequential_f64": value / v64,
-            "rel_l2_f32_vs_f64": {"median": float(np.median(errs)), "max": float(np.max(errs))}}
+            "rel_l2_f32_vs_f64": {"median": float(np.median(errs)), "max": float(np.max(errs)),
+                                  "normalised_by": "L2 norm of the initial field"}}
     print(json.dumps(line), flush=True)
 
 

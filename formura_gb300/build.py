@@ -65,19 +65,28 @@ def generate(names: Optional[List[str]] = None) -> Dict[str, str]:
     from .generator.manifest import compile_program
     os.makedirs(GEN, exist_ok=True)
     out = {}
+    registered: List[str] = []
     for name in names or program_names():
         src, cfg = program_sources(name)
         mm = compile_program(src, decode_config(cfg))
         kp = emit_cuda(mm, name, runtime_params(cfg))
+        text = kp.source
+        subs = []
+        for graph in ("first_step", "filter"):
+            if getattr(mm, graph) is not None:
+                sub = emit_cuda(mm, name, runtime_params(cfg), graph)
+                text += "\n" + sub.source
+                subs.append(f"{name}__{graph}")
         path = os.path.join(GEN, f"prog_{name}.cu")
-        _write_if_changed(path, kp.source)
+        _write_if_changed(path, text)
         meta = {"name": name, "fields": kp.fields, "dim": kp.dim, "sleeve": kp.sleeve,
                 "shift": kp.shift, "nuniforms": len(kp.uniform_exprs),
-                "stages": len(kp.stages), "mids": len(kp.mids)}
+                "stages": len(kp.stages), "mids": len(kp.mids), "subprograms": subs}
         _write_if_changed(os.path.join(GEN, f"prog_{name}.json"), json.dumps(meta, indent=1) + "\n")
         out[name] = path
+        registered.extend([name] + subs)
     reg = ['#include "../csrc/fgb_internal.h"']
-    names = sorted(out)
+    names = sorted(registered)
     reg += [f'extern "C" const FgbProgramDesc* fgb_program_{n}(void);' for n in names]
     reg.append('extern "C" const FgbProgramGetter fgb_builtin_programs[] = {'
                + ", ".join(f"&fgb_program_{n}" for n in names) + "};")

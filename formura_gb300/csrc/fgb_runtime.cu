@@ -76,6 +76,26 @@ __global__ void from_storage(const S* __restrict__ src, double* __restrict__ dst
   }
 }
 
+// FP64 sums of every field (conserved totals), whatever the storage type.
+// One partial sum per block in FP64, then the host adds the partials in a
+// fixed order, so the result does not depend on scheduling.
+template <class S>
+__global__ void field_partial_sums(const S* __restrict__ a, size_t n, double* __restrict__ partial) {
+  __shared__ double red[256];
+  double acc = 0.0;
+  for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+    if constexpr (sizeof(S) == 2) acc += (double)__half2float(a[i]);
+    else acc += (double)a[i];
+  }
+  red[threadIdx.x] = acc;
+  __syncthreads();
+  for (int w = blockDim.x / 2; w > 0; w >>= 1) {
+    if ((int)threadIdx.x < w) red[threadIdx.x] += red[threadIdx.x + w];
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) partial[blockIdx.x] = red[0];
+}
+
 }  // namespace
 
 struct fgb_grid {
@@ -100,6 +120,12 @@ struct fgb_grid {
   std::vector<void*> snaps;             // checkpoints of the forward state
   int grad_steps = -1;                  // steps recorded by fgb_gradient_forward
   int64_t grad_fwd = 0, grad_adj = 0;   // forward steps (incl. recomputation) and adjoint steps
+  // first_step / filter functions of the program (Templates.hs:252-270)
+  struct Sub {
+    const FgbProgramDesc* prog = nullptr;
+    void* uniforms = nullptr;
+    void* mids = nullptr;
+  } sub[2];
 };
 
 static const int kGraphSteps = 16;
@@ -243,6 +269,10 @@ int fgb_close(fgb_grid* g) {
   cudaFree(g->staging);
   cudaFree(g->lam[0]);
   cudaFree(g->lam[1]);
+  for (auto& sb : g->sub) {
+    cudaFree(sb.uniforms);
+    cudaFree(sb.mids);
+  }
   free_snaps(g);
   if (g->stream) cudaStreamDestroy(g->stream);
   delete g;
@@ -624,6 +654,92 @@ int fgb_gradient_stats(fgb_grid* g, int64_t* forward_steps, int64_t* adjoint_ste
   if (!g) return fail(FGB_E_ARG, "null grid");
   if (forward_steps) *forward_steps = g->grad_fwd;
   if (adjoint_steps) *adjoint_steps = g->grad_adj;
+  return FGB_OK;
+}
+
+static int sub_index(const char* which) {
+  if (!which) return -1;
+  if (strcmp(which, "first_step") == 0) return 0;
+  if (strcmp(which, "filter") == 0) return 1;
+  return -1;
+}
+
+int fgb_attach(fgb_grid* g, const char* which, const double* uniforms, int nuniforms) {
+  const int k = sub_index(which);
+  if (!g || k < 0) return fail(FGB_E_ARG, "attach: expected \"first_step\" or \"filter\"");
+  char name[256];
+  snprintf(name, sizeof name, "%s__%s", g->prog->name, which);
+  const FgbProgramDesc* d = find_program(name);
+  if (!d) return fail(FGB_E_PROGRAM, "program %s has no %s function in this library", g->prog->name, which);
+  if (d->nfields != g->prog->nfields || d->dim != g->prog->dim)
+    return fail(FGB_E_ARG, "%s does not match the step's state", name);
+  if (nuniforms != d->nuniforms || (nuniforms > 0 && !uniforms))
+    return fail(FGB_E_ARG, "%s needs %d uniform values, got %d", name, d->nuniforms, nuniforms);
+  for (int a = 0; a < 3; ++a) {
+    const int need = d->reach > d->shift ? d->reach : d->shift;
+    if (g->n[a] > 1 && g->n[a] < need) return fail(FGB_E_ARG, "grid too small for %s", name);
+  }
+  fgb_grid::Sub& s = g->sub[k];
+  cudaFree(s.uniforms);
+  cudaFree(s.mids);
+  s = fgb_grid::Sub();
+  const size_t cs = compute_size(g->precision);
+  if (d->nuniforms > 0) {
+    FGB_CUDA(cudaMalloc(&s.uniforms, d->nuniforms * cs), "attach");
+    if (cs == 8) {
+      FGB_CUDA(cudaMemcpy(s.uniforms, uniforms, d->nuniforms * 8, cudaMemcpyHostToDevice), "attach");
+    } else {
+      std::vector<float> u(uniforms, uniforms + d->nuniforms);
+      FGB_CUDA(cudaMemcpy(s.uniforms, u.data(), u.size() * 4, cudaMemcpyHostToDevice), "attach");
+    }
+  }
+  if (d->nmids > 0) FGB_CUDA(cudaMalloc(&s.mids, g->cells * d->nmids * cs), "attach");
+  s.prog = d;
+  return FGB_OK;
+}
+
+int fgb_apply(fgb_grid* g, const char* which) {
+  const int k = sub_index(which);
+  if (!g || k < 0 || !g->sub[k].prog) return fail(FGB_E_ARG, "%s is not attached", which ? which : "(null)");
+  const fgb_grid::Sub& s = g->sub[k];
+  FgbLaunch L;
+  fill_launch(g, g->cur, &L);
+  const size_t cs = compute_size(g->precision);
+  for (int m = 0; m < s.prog->nmids; ++m) L.mid[m] = (char*)s.mids + m * g->cells * cs;
+  L.uniforms = s.uniforms;
+  for (int st = 0; st < s.prog->nstages; ++st) {
+    cudaError_t e = s.prog->launch[g->precision][st](&L, g->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "apply");
+    ++g->launches;
+  }
+  g->cur ^= 1;
+  return FGB_OK;
+}
+
+int fgb_totals(fgb_grid* g, double* sums, int nfields) {
+  if (!g || !sums || nfields != g->prog->nfields) return fail(FGB_E_ARG, "bad totals arguments");
+  const int blocks = 608;   // 4 per SM on 152 SMs
+  double* partial = nullptr;
+  FGB_CUDA(cudaMalloc(&partial, (size_t)blocks * nfields * sizeof(double)), "totals");
+  const size_t es = storage_size(g->precision);
+  for (int f = 0; f < nfields; ++f) {
+    const void* a = (const char*)g->state[g->cur] + f * g->cells * es;
+    double* p = partial + (size_t)f * blocks;
+    if (es == 8) field_partial_sums<double><<<blocks, 256, 0, g->stream>>>((const double*)a, g->cells, p);
+    else if (es == 4) field_partial_sums<float><<<blocks, 256, 0, g->stream>>>((const float*)a, g->cells, p);
+    else field_partial_sums<__half><<<blocks, 256, 0, g->stream>>>((const __half*)a, g->cells, p);
+    ++g->launches;
+  }
+  std::vector<double> h((size_t)blocks * nfields);
+  cudaError_t e = cudaMemcpyAsync(h.data(), partial, h.size() * sizeof(double), cudaMemcpyDeviceToHost, g->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
+  cudaFree(partial);
+  if (e != cudaSuccess) return cuda_fail(e, "totals");
+  for (int f = 0; f < nfields; ++f) {
+    double s = 0.0;
+    for (int b = 0; b < blocks; ++b) s += h[(size_t)f * blocks + b];
+    sums[f] = f < (int)FGB_MAX_FIELDS && g->precision == FGB_F16 ? s * g->scale[f] : s;
+  }
   return FGB_OK;
 }
 

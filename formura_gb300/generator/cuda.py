@@ -190,9 +190,10 @@ class _Analysis:
     """Classifies micro nodes of one program: grid-independent (uniform) or
     not, and whether a uniform value depends on the configuration."""
 
-    def __init__(self, mm: MMProgram, runtime_params: List[str]):
+    def __init__(self, mm: MMProgram, runtime_params: List[str], graph: str = "step"):
         self.mm = mm
-        self.g = mm.om.step_graph
+        self.g = {"step": mm.om.step_graph, "first_step": mm.om.first_step_graph,
+                  "filter": mm.om.filter_graph}[graph]
         self.axes = mm.om.genv.axes
         names = {"d" + a for a in self.axes} | {"total_grid_" + a for a in self.axes}
         names |= set(runtime_params)
@@ -478,22 +479,28 @@ class _StageEmitter:
 
 
 class _ProgramEmitter:
-    def __init__(self, mm: MMProgram, name: str, runtime_params: List[str]):
+    def __init__(self, mm: MMProgram, name: str, runtime_params: List[str], graph: str = "step"):
         self.mm = mm
         self.name = name
+        self.graph = graph
         self.dim = mm.om.genv.dimension
         if self.dim > 3:
             raise FormuraCompileError("the GPU backend supports 1, 2 and 3 dimensions")
         self.fields = mm.fields
-        self.an = _Analysis(mm, runtime_params)
+        self.an = _Analysis(mm, runtime_params, graph)
         self.runtime_params = list(runtime_params)
-        self.stages = build_stages(mm.step)
+        cfg = mm.om.config
+        self.mmg = {"step": mm.step, "first_step": mm.first_step, "filter": mm.filter}[graph]
+        self.sleeve = {"step": cfg.sleeve, "first_step": cfg.sleeve0, "filter": cfg.filter_sleeve}[graph]
+        if self.mmg is None:
+            raise FormuraCompileError(f"the program has no {graph} function")
+        self.stages = build_stages(self.mmg)
         self.mids = sorted({m for s in self.stages for m in s.mid_out})
         self.table: List[tuple] = []
         self.scaled_cache: Dict[int, dict] = {}
-        rng = calc_range(mm.step)
-        s = mm.om.config.sleeve
-        stores = [n for n in mm.step if n.is_store]
+        rng = calc_range(self.mmg)
+        s = self.sleeve
+        stores = [n for n in self.mmg if n.is_store]
         offs = {rng[n.omid].offset() for n in stores}
         sizes = {rng[n.omid].size() for n in stores}
         if len(offs) != 1 or sizes != {2 * s}:
@@ -502,7 +509,7 @@ class _ProgramEmitter:
                 "reference's loop nest would write outside the grid")
         self.shift = 2 * s - offs.pop()
         reach = 0
-        for n in mm.step:
+        for n in self.mmg:
             for mn in n.micro:
                 if mn.inst[0] in ("loadstatic", "loadcursor"):
                     reach = max(reach, max(abs(x) for x in mn.inst[1]))
@@ -538,7 +545,7 @@ class _ProgramEmitter:
                 f"    using T = typename M::T;\n"
                 f"    (void)U;\n{body}\n  }}\n}};\n")
         adj_src = None
-        if len(self.stages) == 1 and not self.mids:
+        if self.graph == "step" and len(self.stages) == 1 and not self.mids:
             from .adjoint import emit_adjoint
             try:
                 adj_src, _ = emit_adjoint(self.mm, self.name, self)
@@ -552,7 +559,7 @@ class _ProgramEmitter:
                    f"  static constexpr int kFields = {len(self.fields)};\n"
                    f"  static constexpr int kMids = {len(self.mids)};\n"
                    f"  static constexpr int kStages = {len(self.stages)};\n"
-                   f"  static constexpr int kSleeve = {self.mm.om.config.sleeve};\n"
+                   f"  static constexpr int kSleeve = {self.sleeve};\n"
                    f"  static constexpr int kShift = {self.shift};\n"
                    f"  static constexpr int kReach = {self.reach};\n"
                    f"  static constexpr int kUniforms = {len(self.table)};\n"
@@ -564,12 +571,18 @@ class _ProgramEmitter:
         out.append(f"static const char* const fgb_fields_{self.name}[] = {{{names}}};")
         out.append(f"FGB_DEFINE_PROGRAM({self.name}, fgb_gen_{self.name}::Prog, fgb_fields_{self.name}, {stage_list})")
         return KernelProgram(self.name, self.dim, list(self.mm.om.genv.axes), list(self.fields),
-                             self.mm.om.config.sleeve, self.shift, self.reach, self.stages,
+                             self.sleeve, self.shift, self.reach, self.stages,
                              self.mids, list(self.table), self.runtime_params, "\n".join(out) + "\n")
 
 
-def emit_cuda(mm: MMProgram, name: str, runtime_params: Optional[List[str]] = None) -> KernelProgram:
-    return _ProgramEmitter(mm, name, runtime_params or []).emit()
+def emit_cuda(mm: MMProgram, name: str, runtime_params: Optional[List[str]] = None,
+              graph: str = "step") -> KernelProgram:
+    """Device code of the step function (or of first_step / filter, which
+    become library programs named <name>__first_step / <name>__filter)."""
+    kp = _ProgramEmitter(mm, name if graph == "step" else f"{name}__{graph}",
+                         runtime_params or [], graph).emit()
+    kp.graph = graph
+    return kp
 
 
 def eval_utree(an: "_Analysis", tree, params=None) -> float:
@@ -591,7 +604,7 @@ def eval_utree(an: "_Analysis", tree, params=None) -> float:
 
 def uniform_table(mm: MMProgram, kp: KernelProgram, params: Optional[Dict[str, float]] = None) -> List[float]:
     """Host values of the runtime uniform table for one configuration."""
-    an = _Analysis(mm, kp.runtime_params)
+    an = _Analysis(mm, kp.runtime_params, getattr(kp, "graph", "step"))
     out = []
     for entry in kp.uniform_exprs:
         kind = entry[0]

@@ -104,13 +104,16 @@ def emit_dropin(mm: MMProgram, program: str, header_name: str,
                 runtime_params: Optional[List[str]] = None) -> Tuple[str, str]:
     """Return (X.h, X.c) for the GB300 backend; ``program`` is the name of
     the program compiled into libformura_gb300."""
-    if mm.first_step is not None or mm.filter is not None:
-        raise FormuraCompileError("first_step and filter are not supported by the GPU backend yet")
     cfg = mm.om.config
     if cfg.mpi_shape is not None and any(m != 1 for m in cfg.mpi_shape):
         raise FormuraCompileError("the GPU backend runs one rank per process (mpi_shape must be all 1)")
     kp = emit_cuda(mm, program, runtime_params or [])
     U = uniform_table(mm, kp, params)
+    subs = {}
+    for graph in ("first_step", "filter"):
+        if getattr(mm, graph) is not None:
+            kps = emit_cuda(mm, program, runtime_params or [], graph)
+            subs[graph] = uniform_table(mm, kps, params)
     axes = mm.om.genv.axes
     N = list(cfg.grid_per_node)
     dim = len(N)
@@ -181,22 +184,50 @@ def emit_dropin(mm: MMProgram, program: str, header_name: str,
     tune = cfg.gpu.get("gpu_autotune", 1)
     if int(tune):
         c.append(f'formura_gb300_check(fgb_autotune(formura_gb300_grid, {max(8, 2 * nt) if nt < 64 else 64}, 0), "fgb_autotune");')
+    for graph, Ug in subs.items():
+        c.append(f"static const double formura_gb300_{graph}_uniforms[{max(1, len(Ug))}] = {{"
+                 + ", ".join(c_double(x) for x in Ug) + ("" if Ug else "0.0") + "};")
+        c.append(f'formura_gb300_check(fgb_attach(formura_gb300_grid, "{graph}", formura_gb300_{graph}_uniforms, '
+                 f'{len(Ug)}), "fgb_attach");')
+    if "first_step" in subs:
+        # Formura_First_Step (Templates.hs:250, 252-260): once, rolled by its sleeve
+        c.append(f'formura_gb300_check(fgb_upload(formura_gb300_grid, (const double*)&{gsn}), "fgb_upload");')
+        c.append('formura_gb300_check(fgb_apply(formura_gb300_grid, "first_step"), "fgb_apply");')
+        c.append(f'formura_gb300_check(fgb_download(formura_gb300_grid, (double*)&{gsn}), "fgb_download");')
+        for a in axes:
+            c.append(f"n->offset_{a} = (n->offset_{a} - {cfg.sleeve0} + n->total_grid_{a})%n->total_grid_{a};")
     c.append(f"fgb_host_register(&{gsn}, sizeof({gsn}));")
     c.append("}")
+    # one reference Formura_Forward call advances g steps (Templates.hs:300-334);
+    # a call here advances nt = k*g steps and keeps the reference's per-call
+    # offset, filter and time_step updates for each of the k sub-calls
+    g = cfg.blocking.nt if cfg.blocking.temporal else 1
+    if nt % g != 0:
+        raise FormuraCompileError(f"gpu_steps_per_forward must be a multiple of {g}")
+    k = nt // g
+
+    def offsets(amount):
+        return [f"n->offset_{a} = (n->offset_{a} - {amount} + n->total_grid_{a})%n->total_grid_{a};" for a in axes]
+
     c.append("void Formura_Forward(Formura_Navi *n) {")
     c.append(f'formura_gb300_check(fgb_upload(formura_gb300_grid, (const double*)&{gsn}), "fgb_upload");')
-    c.append(f'formura_gb300_check(fgb_forward(formura_gb300_grid, {nt}), "fgb_forward");')
+    if "filter" in subs:
+        c.append(f"for (int c = 0; c < {k}; ++c) {{")
+        c.append(f'formura_gb300_check(fgb_forward(formura_gb300_grid, {g}), "fgb_forward");')
+        c += offsets(s * g)
+        c.append(f"if (n->time_step % {cfg.filter_interval} == 0) {{")
+        c.append('formura_gb300_check(fgb_apply(formura_gb300_grid, "filter"), "fgb_apply");')
+        c += offsets(cfg.filter_sleeve)
+        c.append("}")
+        c.append(f"n->time_step += {g};")
+        c.append("}")
+    else:
+        c.append(f'formura_gb300_check(fgb_forward(formura_gb300_grid, {nt}), "fgb_forward");')
+        c.append(f"for (int c = 0; c < {k}; ++c) {{")
+        c += offsets(s * g)
+        c.append(f"n->time_step += {g};")
+        c.append("}")
     c.append(f'formura_gb300_check(fgb_download(formura_gb300_grid, (double*)&{gsn}), "fgb_download");')
-    tb_nt = cfg.blocking.nt if cfg.blocking.temporal else 1
-    for a in axes:
-        if nt == tb_nt:
-            # the reference's own update (Templates.hs:328 and :346)
-            c.append(f"n->offset_{a} = (n->offset_{a} - {s * nt} + n->total_grid_{a})%n->total_grid_{a};")
-        else:
-            # gpu_steps_per_forward: the same as nt single-step updates
-            c.append(f"n->offset_{a} = ((n->offset_{a} - {s * nt}) % n->total_grid_{a} + n->total_grid_{a})"
-                     f"%n->total_grid_{a};")
-    c.append(f"n->time_step += {nt};")
     c.append("}")
     c.append("void Formura_Finalize() {")
     c.append(f"if (formura_gb300_grid) {{ fgb_host_unregister(&{gsn}); fgb_close(formura_gb300_grid); formura_gb300_grid = 0; }}")

@@ -76,6 +76,7 @@ class Library:
         L.fgb_gradient_backward_device.argtypes = [ctypes.c_void_p, ctypes.c_void_p, ctypes.c_void_p]
         L.fgb_gradient_stats.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_int64), ctypes.POINTER(ctypes.c_int64)]
         L.fgb_adjoint_steps.argtypes = [ctypes.c_void_p, ctypes.c_int]
+        L.fgb_totals.argtypes = [ctypes.c_void_p, ctypes.POINTER(ctypes.c_double), ctypes.c_int]
 
     @classmethod
     def get(cls) -> "Library":
@@ -165,6 +166,12 @@ class Grid:
         c = ctypes.c_int()
         self.L.check(self.L.lib.fgb_autotune(self.h, int(trial_steps), ctypes.byref(c)), "fgb_autotune")
         return c.value
+
+    def totals(self) -> np.ndarray:
+        """FP64 sum of each field of the current state."""
+        out = (ctypes.c_double * self.nfields)()
+        self.L.check(self.L.lib.fgb_totals(self.h, out, self.nfields), "fgb_totals")
+        return np.array(out[:])
 
     # -- reverse mode -----------------------------------------------------
     def backward(self, lam_next: np.ndarray) -> np.ndarray:

@@ -126,3 +126,20 @@ def gs_square_state(n: int, seed: int) -> np.ndarray:
     sq = inside[:, None] & inside[None, :]
     st = gs_perturb(np.where(sq, 0.5, 1.0), np.where(sq, 0.25, 0.0), seed)
     return np.stack([st["u"], st["v"]])
+
+
+def mhd_config(n: int = 64, length: float = 1.0, extra: str = "") -> str:
+    return hllc_config(n, length, extra)
+
+
+def mhd_state(shape: Tuple[int, int, int], seed: int = 0) -> Dict[str, np.ndarray]:
+    """Ideal-MHD initial state: the compressible Euler state of hllc_state
+    plus a magnetic field B = (0.3, 0, 0) + 0.05 * N(0, 1) per component,
+    psi = 0, and the magnetic energy added to e."""
+    st = hllc_state(shape, seed)
+    rng = np.random.default_rng(seed + 7919)
+    b = {"bx": 0.3 + 0.05 * rng.standard_normal(shape), "by": 0.05 * rng.standard_normal(shape),
+         "bz": 0.05 * rng.standard_normal(shape), "psi": np.zeros(shape)}
+    st["e"] = st["e"] + 0.5 * (b["bx"] ** 2 + b["by"] ** 2 + b["bz"] ** 2)
+    st.update(b)
+    return st

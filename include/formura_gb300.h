@@ -146,6 +146,18 @@ int fgb_batch_autotune(fgb_batch* batch, int trial_steps, int* chosen);
 void* fgb_batch_stream(fgb_batch* batch);
 int64_t fgb_batch_launch_count(fgb_batch* batch);
 
+/* The program's first_step and filter functions (Templates.hs:252-270).
+ * fgb_attach(grid, "first_step" | "filter", uniforms, n) loads the function
+ * with its own uniform table; fgb_apply runs it once on the current state,
+ * with its own roll (its sleeve), as Formura_First_Step / Formura_Filter do. */
+int fgb_attach(fgb_grid* grid, const char* which, const double* uniforms, int nuniforms);
+int fgb_apply(fgb_grid* grid, const char* which);
+
+/* FP64 sum of every state field of the current state (conserved totals of
+ * mass, momentum and energy for conservative programs), whatever the
+ * storage precision; deterministic for a given grid size. */
+int fgb_totals(fgb_grid* grid, double* sums, int nfields);
+
 /* Pin a host range (e.g. formura_data) for faster copies; optional. */
 int fgb_host_register(void* ptr, size_t bytes);
 int fgb_host_unregister(void* ptr);

@@ -4,11 +4,12 @@ programs, run through the restated Formura generator (the oracle):
 * examples/diffusion3/diffusion3.fmr on a 16^3 grid (heat workload);
 * examples/pearson2/pearson2.fmr with the Gray-Scott workload's feed rate
   f = 0.04 (the other parameters already match) on 64^2;
-* sample/3d_hllc/3d_hllc.fmr with Courant number 0.4 on 16^3.
+* sample/3d_hllc/3d_hllc.fmr with Courant number 0.4 on 16^3;
+* sample/mhd_3d_hlld/mhd_3d_hlld.fmr on 12^3 (magnetised random state).
 
 Each fixture stores the seeded input state, the config, the step count and
 the output state and grid offset.  The shipped programs (heat3d, gs2d,
-hllc3d) must reproduce them bit for bit.  Needs the reference tree; run from
+hllc3d, hlld3d) must reproduce them bit for bit.  Needs the reference tree; run from
 the repository root:  python tests/golden/make_golden.py
 """
 import os
@@ -61,3 +62,7 @@ if __name__ == "__main__":
                                          [("double :: C_cfl = 0.8", "double :: C_cfl = 0.4")]),
          W.hllc_config(16), 5, lambda r: W.hllc_state((16, 16, 16), 13),
          {"e": "e", "mx": "rhou", "my": "rhov", "mz": "rhow", "rho": "rho"})
+    make("hlld3d_12_3", reference_source("sample/mhd_3d_hlld/mhd_3d_hlld.fmr"), W.mhd_config(12), 3,
+         lambda r: W.mhd_state((12, 12, 12), 14),
+         {"bx": "B_x", "by": "B_y", "bz": "B_z", "e": "e", "mx": "rhou", "my": "rhov", "mz": "rhow",
+          "psi": "psi", "rho": "rho"})

@@ -133,7 +133,7 @@ GOLDEN = __import__("os").path.join(__import__("os").path.dirname(__import__("os
 
 
 @pytest.mark.parametrize("name,program", [("heat3d_16_10", "heat3d"), ("gs2d_64_50", "gs2d"),
-                                          ("hllc3d_16_5", "hllc3d")])
+                                          ("hllc3d_16_5", "hllc3d"), ("hlld3d_12_3", "hlld3d")])
 def test_gpu_reproduces_reference_program_fixture(name, program):
     """The GPU reproduces, bit for bit, the output of the reference's own
     example program (diffusion3 / pearson2 / 3d_hllc) on the same input."""
@@ -191,3 +191,44 @@ def test_hllc_f32_storage():
         err = W.rel_l2(gpu.get(f), ref.get(f))
         assert err < 1e-5, f"{f}: rel-L2 {err}"
     gpu.finalize()
+
+
+def test_hlld_f64_bit_exact():
+    n, steps = 20, 6
+    cfg = W.mhd_config(n)
+    ref, gpu = _pair("hlld3d", cfg, "gpu_steps_per_forward: 3\n", "n20")
+    ref.init()
+    gpu.init()
+    st = W.mhd_state((n, n, n), seed=3)
+    for f in ref.fields:
+        ref.set(f, st[f])
+        gpu.set(f, st[f])
+    for _ in range(steps // 3):
+        ref.forward(3)
+        gpu.forward(1)
+    _check_navi(ref.navi_dict(), gpu.navi_dict())
+    for f in ref.fields:
+        assert np.array_equal(ref.get(f), gpu.get(f)), f
+    gpu.finalize()
+
+
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_hllc_conserved_totals_fp64(prec):
+    """FP64 totals of mass, momentum and energy over 50 steps of HLLC (FP64
+    reductions also for FP32 storage)."""
+    from formura_gb300.host import Grid, program_uniforms
+    n = 32
+    src, _ = builtin_program("hllc3d")
+    _, U = program_uniforms(src, W.hllc_config(n), "hllc3d")
+    st = W.hllc_state((n, n, n), seed=8)
+    x = np.stack([st[f] for f in ("e", "mx", "my", "mz", "rho")])
+    g = Grid("hllc3d", (n, n, n), prec, U)
+    g.upload(x)
+    t0 = g.totals()
+    assert np.allclose(t0, x.reshape(5, -1).sum(axis=1), rtol=1e-12 if prec == "f64" else 1e-6, atol=1e-9)
+    g.forward(50)
+    t1 = g.totals()
+    scale = np.abs(x).reshape(5, -1).sum(axis=1)
+    drift = np.abs(t1 - t0) / scale
+    assert (drift < (1e-13 if prec == "f64" else 1e-5)).all(), drift
+    g.close()

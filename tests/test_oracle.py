@@ -96,7 +96,7 @@ def test_temporal_blocking_equals_no_blocking():
 
 
 @pytest.mark.parametrize("name,program", [("heat3d_16_10", "heat3d"), ("gs2d_64_50", "gs2d"),
-                                          ("hllc3d_16_5", "hllc3d")])
+                                          ("hllc3d_16_5", "hllc3d"), ("hlld3d_12_3", "hlld3d")])
 def test_golden_fixture_reproduced(name, program):
     """The shipped programs reproduce, bit for bit, the reference's own
     example programs (fixtures made by tests/golden/make_golden.py)."""
