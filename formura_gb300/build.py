@@ -137,6 +137,7 @@ def build(names: Optional[List[str]] = None, jobs: Optional[int] = None, verbose
     units = [(os.path.join(CSRC, "fgb_runtime.cu"), os.path.join(BUILD, "fgb_runtime.o")),
              (os.path.join(CSRC, "fgb_noalloc.cu"), os.path.join(BUILD, "fgb_noalloc.o")),
              (os.path.join(CSRC, "fgb_batch.cu"), os.path.join(BUILD, "fgb_batch.o")),
+             (os.path.join(CSRC, "fgb_lazy.cu"), os.path.join(BUILD, "fgb_lazy.o")),
              (os.path.join(GEN, "fgb_registry.cu"), os.path.join(BUILD, "fgb_registry.o"))]
     units += [(p, os.path.join(BUILD, f"prog_{n}.o")) for n, p in gen.items()]
     jobs = jobs or max(2, min(len(units), os.cpu_count() or 4))

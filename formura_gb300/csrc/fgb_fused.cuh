@@ -54,6 +54,13 @@ __device__ __forceinline__ int pmod(int a, int n) {
   return r < 0 ? r + n : r;
 }
 
+// Periodic index for -n <= a < 2n (tile halos are shorter than the grid):
+// a compare and an add instead of an integer division.
+__device__ __forceinline__ int pwrap(int a, int n) {
+  a += a < 0 ? n : 0;
+  return a >= n ? a - n : a;
+}
+
 template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY, int RB>
 __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ FgbLaunch L) {
   using T = typename M::T;
@@ -68,11 +75,13 @@ __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ F
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const T* __restrict__ U = static_cast<const T*>(L.uniforms);
 
-  // load the tile and its halo (periodic)
+  // load the tile and its halo (periodic); halos shorter than the grid use
+  // the cheap wrap
+  const bool small = TY + H >= ny || TX + H >= nx || K * Prog::kShift >= ny || K * Prog::kShift >= nx;
   for (int ly = threadIdx.y; ly < RY; ly += BY) {
-    const int gy = pmod(y0 - H + ly, ny);
+    const int gy = small ? pmod(y0 - H + ly, ny) : pwrap(y0 - H + ly, ny);
     for (int lx = threadIdx.x; lx < RX; lx += BX) {
-      const int gx = pmod(x0 - H + lx, nx);
+      const int gx = small ? pmod(x0 - H + lx, nx) : pwrap(x0 - H + lx, nx);
       const uint32_t g = (uint32_t)gy * (uint32_t)nx + (uint32_t)gx;
 #pragma unroll
       for (int f = 0; f < NF; ++f)
@@ -121,11 +130,11 @@ __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ F
   for (int ty = threadIdx.y; ty < TY; ty += BY) {
     const int py = y0 + ty;
     if (py >= ny) break;
-    const int oy = (py + K * Prog::kShift) % ny;
+    const int oy = small ? (py + K * Prog::kShift) % ny : pwrap(py + K * Prog::kShift, ny);
     for (int tx = threadIdx.x; tx < TX; tx += BX) {
       const int px = x0 + tx;
       if (px >= nx) break;
-      const int ox = (px + K * Prog::kShift) % nx;
+      const int ox = small ? (px + K * Prog::kShift) % nx : pwrap(px + K * Prog::kShift, nx);
       const uint32_t g = (uint32_t)oy * (uint32_t)nx + (uint32_t)ox;
 #pragma unroll
       for (int f = 0; f < NF; ++f)
@@ -189,10 +198,11 @@ __global__ void __launch_bounds__(BX * BY) tb2d_batch_kernel(const __grid_consta
     S* dst = static_cast<S*>(in.state[B.parity ^ 1]);
     const T* __restrict__ U = static_cast<const T*>(in.uniforms);
     const int x0 = tile.x0, y0 = tile.y0;
+    const bool small = TY + H >= ny || TX + H >= nx || K * Prog::kShift >= ny || K * Prog::kShift >= nx;
     for (int ly = threadIdx.y; ly < RY; ly += BY) {
-      const int gy = pmod(y0 - H + ly, ny);
+      const int gy = small ? pmod(y0 - H + ly, ny) : pwrap(y0 - H + ly, ny);
       for (int lx = threadIdx.x; lx < RX; lx += BX) {
-        const int gx = pmod(x0 - H + lx, nx);
+        const int gx = small ? pmod(x0 - H + lx, nx) : pwrap(x0 - H + lx, nx);
         const size_t g = (size_t)gy * nx + gx;
 #pragma unroll
         for (int f = 0; f < NF; ++f)
@@ -217,11 +227,11 @@ __global__ void __launch_bounds__(BX * BY) tb2d_batch_kernel(const __grid_consta
     for (int ty = threadIdx.y; ty < TY; ty += BY) {
       const int py = y0 + ty;
       if (py >= ny) break;
-      const int oy = (py + K * Prog::kShift) % ny;
+      const int oy = small ? (py + K * Prog::kShift) % ny : pwrap(py + K * Prog::kShift, ny);
       for (int tx = threadIdx.x; tx < TX; tx += BX) {
         const int px = x0 + tx;
         if (px >= nx) break;
-        const int ox = (px + K * Prog::kShift) % nx;
+        const int ox = small ? (px + K * Prog::kShift) % nx : pwrap(px + K * Prog::kShift, nx);
         const size_t g = (size_t)oy * nx + ox;
 #pragma unroll
         for (int f = 0; f < NF; ++f)

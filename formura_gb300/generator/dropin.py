@@ -15,7 +15,9 @@ Backend options come from ``gpu_*`` keys of the numerical config:
 ``gpu_precision`` (f64, f64fast, f32, f16), ``gpu_steps_per_forward``
 (default: ``temporal_blocking_interval`` when temporal blocking is
 configured, else 1, i.e. the reference's step count per call) and
-``gpu_field_scales`` (FP16 storage) and ``gpu_autotune`` (0 turns off the
+``gpu_field_scales`` (FP16 storage), ``gpu_host_sync`` (``eager``: upload and
+download formura_data on every call; ``lazy``: copy only when the driver
+touches it, by page protection) and ``gpu_autotune`` (0 turns off the
 choice of the temporal-blocking kernel at ``Formura_Init``; results do not
 depend on it except with FP16 storage).
 """
@@ -150,8 +152,22 @@ def emit_dropin(mm: MMProgram, program: str, header_name: str,
           "void Formura_Finalize();"]
 
     scales = cfg.gpu.get("gpu_field_scales")
-    c = [f'#include "{header_name}"', '#include "formura_gb300.h"',
-         f"{gst} {gsn};",
+    sync = str(cfg.gpu.get("gpu_host_sync", "eager"))
+    if sync not in ("eager", "lazy"):
+        raise FormuraCompileError("gpu_host_sync must be eager or lazy")
+    lazy = sync == "lazy"
+    if lazy:
+        # formura_data in its own page-aligned, page-padded block (64 KiB
+        # covers 4 KiB and 64 KiB pages), so that protecting it protects
+        # nothing else
+        storage = [f"#define FORMURA_GB300_PAGE 65536",
+                   f"static union {{ {gst} s; char pad[(sizeof({gst}) + FORMURA_GB300_PAGE - 1)"
+                   f" / FORMURA_GB300_PAGE * FORMURA_GB300_PAGE]; }} formura_gb300_storage"
+                   f" __attribute__((aligned(FORMURA_GB300_PAGE)));",
+                   f'extern {gst} {gsn} __attribute__((alias("formura_gb300_storage")));']
+    else:
+        storage = [f"{gst} {gsn};"]
+    c = [f'#include "{header_name}"', '#include "formura_gb300.h"'] + storage + [
          "static fgb_grid* formura_gb300_grid = 0;",
          f"static const double formura_gb300_uniforms[{max(1, len(U))}] = {{"
          + ", ".join(c_double(x) for x in U) + ("" if U else "0.0") + "};",
@@ -196,7 +212,11 @@ def emit_dropin(mm: MMProgram, program: str, header_name: str,
         c.append(f'formura_gb300_check(fgb_download(formura_gb300_grid, (double*)&{gsn}), "fgb_download");')
         for a in axes:
             c.append(f"n->offset_{a} = (n->offset_{a} - {cfg.sleeve0} + n->total_grid_{a})%n->total_grid_{a};")
-    c.append(f"fgb_host_register(&{gsn}, sizeof({gsn}));")
+    if lazy:
+        c.append('formura_gb300_check(fgb_lazy_attach(formura_gb300_grid, &formura_gb300_storage, '
+                 'sizeof(formura_gb300_storage)), "fgb_lazy_attach");')
+    else:
+        c.append(f"fgb_host_register(&{gsn}, sizeof({gsn}));")
     c.append("}")
     # one reference Formura_Forward call advances g steps (Templates.hs:300-334);
     # a call here advances nt = k*g steps and keeps the reference's per-call
@@ -210,10 +230,14 @@ def emit_dropin(mm: MMProgram, program: str, header_name: str,
         return [f"n->offset_{a} = (n->offset_{a} - {amount} + n->total_grid_{a})%n->total_grid_{a};" for a in axes]
 
     c.append("void Formura_Forward(Formura_Navi *n) {")
-    c.append(f'formura_gb300_check(fgb_upload(formura_gb300_grid, (const double*)&{gsn}), "fgb_upload");')
+    if lazy:
+        fwd = lambda steps: f'formura_gb300_check(fgb_lazy_forward(formura_gb300_grid, {steps}), "fgb_lazy_forward");'
+    else:
+        c.append(f'formura_gb300_check(fgb_upload(formura_gb300_grid, (const double*)&{gsn}), "fgb_upload");')
+        fwd = lambda steps: f'formura_gb300_check(fgb_forward(formura_gb300_grid, {steps}), "fgb_forward");'
     if "filter" in subs:
         c.append(f"for (int c = 0; c < {k}; ++c) {{")
-        c.append(f'formura_gb300_check(fgb_forward(formura_gb300_grid, {g}), "fgb_forward");')
+        c.append(fwd(g))
         c += offsets(s * g)
         c.append(f"if (n->time_step % {cfg.filter_interval} == 0) {{")
         c.append('formura_gb300_check(fgb_apply(formura_gb300_grid, "filter"), "fgb_apply");')
@@ -222,14 +246,20 @@ def emit_dropin(mm: MMProgram, program: str, header_name: str,
         c.append(f"n->time_step += {g};")
         c.append("}")
     else:
-        c.append(f'formura_gb300_check(fgb_forward(formura_gb300_grid, {nt}), "fgb_forward");')
+        c.append(fwd(nt))
         c.append(f"for (int c = 0; c < {k}; ++c) {{")
         c += offsets(s * g)
         c.append(f"n->time_step += {g};")
         c.append("}")
-    c.append(f'formura_gb300_check(fgb_download(formura_gb300_grid, (double*)&{gsn}), "fgb_download");')
+    if not lazy:
+        c.append(f'formura_gb300_check(fgb_download(formura_gb300_grid, (double*)&{gsn}), "fgb_download");')
     c.append("}")
     c.append("void Formura_Finalize() {")
-    c.append(f"if (formura_gb300_grid) {{ fgb_host_unregister(&{gsn}); fgb_close(formura_gb300_grid); formura_gb300_grid = 0; }}")
+    if lazy:
+        c.append("if (formura_gb300_grid) { fgb_lazy_detach(formura_gb300_grid); fgb_close(formura_gb300_grid); "
+                 "formura_gb300_grid = 0; }")
+    else:
+        c.append(f"if (formura_gb300_grid) {{ fgb_host_unregister(&{gsn}); fgb_close(formura_gb300_grid); "
+                 f"formura_gb300_grid = 0; }}")
     c.append("}")
     return "\n".join(h) + "\n", "\n".join(c) + "\n"

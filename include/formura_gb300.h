@@ -158,6 +158,17 @@ int fgb_apply(fgb_grid* grid, const char* which);
  * storage precision; deterministic for a given grid size. */
 int fgb_totals(fgb_grid* grid, double* sums, int nfields);
 
+/* Lazy host synchronisation (opt-in; the drop-in's gpu_host_sync: lazy).
+ * The host state region (page aligned, whole pages) stays protected while
+ * the device copy is newer; the first access downloads it (SIGSEGV handler,
+ * faults elsewhere go to the previous handler), the first write marks it
+ * dirty, and fgb_lazy_forward uploads only a dirty copy.  fgb_lazy_detach
+ * downloads if needed and unprotects. */
+int fgb_lazy_attach(fgb_grid* grid, void* host_state, size_t bytes);
+int fgb_lazy_forward(fgb_grid* grid, int nsteps);
+int fgb_lazy_detach(fgb_grid* grid);
+int fgb_lazy_stats(fgb_grid* grid, int64_t* uploads, int64_t* downloads);
+
 /* Pin a host range (e.g. formura_data) for faster copies; optional. */
 int fgb_host_register(void* ptr, size_t bytes);
 int fgb_host_unregister(void* ptr);

@@ -225,7 +225,8 @@ def test_hllc_conserved_totals_fp64(prec):
     g = Grid("hllc3d", (n, n, n), prec, U)
     g.upload(x)
     t0 = g.totals()
-    assert np.allclose(t0, x.reshape(5, -1).sum(axis=1), rtol=1e-12 if prec == "f64" else 1e-6, atol=1e-9)
+    stored = x if prec == "f64" else x.astype(np.float32).astype(np.float64)
+    assert np.allclose(t0, stored.reshape(5, -1).sum(axis=1), rtol=1e-12, atol=1e-12)
     g.forward(50)
     t1 = g.totals()
     scale = np.abs(x).reshape(5, -1).sum(axis=1)
