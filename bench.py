@@ -30,6 +30,26 @@ sys.path.insert(0, ROOT)
 HBM_FALLBACK_GBS = 6800.0
 
 
+def W_gs(n):
+    from formura_gb300 import workloads as W
+    return W.gs_config(n)
+
+
+def W_heat(n):
+    from formura_gb300 import workloads as W
+    return W.heat_config(n)
+
+
+def W_hllc(n):
+    from formura_gb300 import workloads as W
+    return W.hllc_config(n)
+
+
+def W_mhd(n):
+    from formura_gb300 import workloads as W
+    return W.mhd_config(n)
+
+
 def measured_peaks():
     p = os.path.join(ROOT, "MEASURED_PEAKS.json")
     if os.path.exists(p):
@@ -224,7 +244,7 @@ def run_ours(args, spec):
     nf = spec["fields"]
     spf = args.spf
     # initial state through the drop-in's Formura_Init (host init function)
-    dp = FormuraProgram(src, spec["cfg"] + f"gpu_steps_per_forward: {spf}\n", spec["program"],
+    dp = FormuraProgram(src, spec["cfg"] + f"gpu_steps_per_forward: {spf}\ngpu_autotune: 0\n", spec["program"],
                         name=f"{spec['program']}_bench_e2e_{local}")
     dp.init()
     st0 = initial_state(spec, dp)
@@ -241,7 +261,11 @@ def run_ours(args, spec):
         return g
 
     g = open_grid(args.precision)
-    tuned = g.autotune(32) if not args.no_autotune else -1
+    if args.variant is not None:
+        g.set_variant(args.variant)
+        tuned = args.variant
+    else:
+        tuned = g.autotune(32) if not args.no_autotune else -1
     variant = next((v for v in g.variants() if v["index"] == tuned), None)
     stream = torch.cuda.ExternalStream(g.stream)
     sampler = ClockSampler(local)
@@ -371,6 +395,8 @@ def main():
     ap.add_argument("--no-variants", action="store_true")
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-autotune", action="store_true")
+    ap.add_argument("--variant", type=int, default=None, help="use this temporal-blocking kernel (no autotune)")
+    ap.add_argument("--size", type=int, default=None, help="grid points per axis (smaller profiling cases)")
     ap.add_argument("--adj-n", type=int, default=512)
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--probes", type=int, default=64)
@@ -385,6 +411,12 @@ def main():
         run_batch(args)
         return
     spec = workload_spec(args.workload)
+    if args.size:
+        n = args.size
+        make = {"gs2d": W_gs, "heat3d": W_heat, "hllc3d": W_hllc, "hlld3d": W_mhd}[args.workload]
+        spec["cfg"] = make(n)
+        spec["shape"] = tuple([n] * len(spec["shape"]))
+        spec["label"] = spec["label"].replace(spec["label"].split(" ")[1], f"{n}^{len(spec['shape'])}", 1)
     if args.steps is None:
         args.steps = max(1, spec["steps_total"] // args.spf) if args.impl == "ours" else 200
     if args.impl == "reference":
