@@ -191,15 +191,17 @@ def run_reference(args, spec):
     print(json.dumps(line), flush=True)
 
 
-def load_traffic(spec, precision):
+def load_traffic(spec, precision, variant=-1):
     """DRAM bytes per launch of the dominant kernel from the committed ncu
-    summary (profiles/traffic.json), or None."""
+    summary (profiles/traffic.json), or None.  Keys are program:precision for
+    the one-step kernel and program:precision:tb<variant> for a fused one."""
     p = os.path.join(ROOT, "profiles", "traffic.json")
     if not os.path.exists(p):
         return None
     with open(p) as f:
         d = json.load(f)
-    return d.get(f"{spec['program']}:{precision}")
+    key = f"{spec['program']}:{precision}" + (f":tb{variant}" if variant >= 0 else "")
+    return d.get(key)
 
 
 def storage_bytes(precision):
@@ -282,20 +284,31 @@ def run_ours(args, spec):
     tsteps = args.steps * spf
     value = ws * cells * tsteps / (ms / 1e3) / 1e9
 
-    # roofline: algorithmic bytes of one time step (read + write of every state
-    # field) over the time of one step; single-stage programs launch one
-    # kernel per step, so this is the per-launch figure of that kernel
-    stages = max(1, launches // max(1, tsteps))
+    # roofline: algorithmic bytes per lattice update (one read and one write
+    # of every state field, no credit for temporal reuse) times the updates
+    # one launch performs, over the launch's average duration.  One-step
+    # kernels update every cell once per launch; a fused kernel of depth K
+    # updates every cell K times, so it can read above 1.0.
     per_step_ms = ms / tsteps
     bytes_per_step = 2 * nf * storage_bytes(args.precision) * cells
+    fused = g.variants()[g.variant]["steps"] if g.variant >= 0 else 1
+    if fused > 1:
+        kernels_per_step = launches / tsteps
+        per_launch = bytes_per_step * fused
+        launch_us = per_step_ms * 1e3 * tsteps / max(1, launches)
+    else:
+        kernels_per_step = max(1, round(launches / max(1, tsteps)))
+        per_launch = bytes_per_step if kernels_per_step == 1 else None
+        launch_us = per_step_ms * 1e3 / kernels_per_step
     peak, peak_kind = measured_peaks()
     achieved = bytes_per_step / (per_step_ms / 1e3) / 1e9
     roofline = {"bound": "hbm", "achieved": achieved, "peak": peak, "unit": "GB/s",
                 "frac": achieved / peak, "peak_source": peak_kind,
-                "traffic": load_traffic(spec, args.precision),
-                "algorithmic_bytes_per_launch": bytes_per_step if stages == 1 else None,
-                "algorithmic_bytes_per_step": bytes_per_step, "kernels_per_step": stages,
-                "avg_step_us": per_step_ms * 1e3}
+                "traffic": load_traffic(spec, args.precision, g.variant),
+                "algorithmic_bytes_per_lattice_update": 2 * nf * storage_bytes(args.precision),
+                "algorithmic_bytes_per_launch": per_launch,
+                "time_steps_per_launch": fused, "kernels_per_step": kernels_per_step,
+                "avg_launch_us": launch_us, "avg_step_us": per_step_ms * 1e3}
 
     # end to end through the drop-in C API: upload + spf steps + download per call
     for _ in range(2):

@@ -69,6 +69,7 @@ __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ F
   constexpr int H = K * R;
   constexpr int RY = TY + 2 * H, RX = TX + 2 * H;
   constexpr int PLANE = RY * RX;
+  static_assert(Prog::kShift >= 0, "the per-step roll is non-negative");
   extern __shared__ __align__(16) unsigned char fgb_smem_raw[];
   T* smem = reinterpret_cast<T*>(fgb_smem_raw);
   const int ny = L.n[1], nx = L.n[2];
@@ -161,8 +162,13 @@ struct Tb2dVariant {
       if (e != cudaSuccess) return e;
       configured = true;
     }
-    dim3 grid((L->n[2] + TX - 1) / TX, (L->n[1] + TY - 1) / TY, 1);
-    kern<<<grid, dim3(BX, BY), kSmem, stream>>>(*L);
+    // enough CTAs to fill the SMs several times over; each chunk re-reads
+    // 2H halo planes, so chunks stay at least 4H planes deep
+    const int gx = (L->n[2] + TX - 1) / TX, gy = (L->n[1] + TY - 1) / TY;
+    const int want = (1216 + gx * gy - 1) / (gx * gy);
+    const int most = L->n[0] / (4 * H) > 1 ? L->n[0] / (4 * H) : 1;
+    const int gz = want < most ? want : most;
+    kern<<<dim3(gx, gy, gz), dim3(BX, BY), kSmem, stream>>>(*L);
     return cudaGetLastError();
   }
   static FgbFusedVariant describe() {
@@ -276,6 +282,151 @@ struct Tb2dBatchVariant {
     FgbBatchVariant v;
     v.launch = &launch;
     v.blocks_per_sm = &blocks_per_sm;
+    v.tile_x = TX;
+    v.tile_y = TY;
+    v.steps = K;
+    v.smem_bytes = kSmem;
+    return v;
+  }
+};
+
+// 3D temporal blocking, 2.5D streaming: a CTA owns an x-y tile (plus a
+// halo of K*R cells) and streams along the slowest axis.  For every level
+// t = 0..K-1 it keeps a ring of 2R+1 planes in shared memory; each new input
+// plane lets every level advance by one plane, and level K is written to
+// HBM directly (rolled by K*shift).  Cursor loads along the streamed axis
+// pick the ring slot, loads across it read the tile.
+template <class T, int NF, int P, int RY, int RX>
+struct PlaneAccess {
+  const T* level;   // ring of the level below: [P][NF][RY][RX]
+  int z, ly, lx;    // plane (position along the streamed axis), tile cell
+  T* res;
+  __device__ __forceinline__ static int slot(int z) {
+    int r = z % P;
+    return r < 0 ? r + P : r;
+  }
+  template <int F, int D0, int D1, int D2>
+  __device__ __forceinline__ T ld() const {
+    return level[((slot(z + D0) * NF + F) * RY + ly + D1) * RX + lx + D2];
+  }
+  template <int F>
+  __device__ __forceinline__ void st(T v) const {
+    res[F] = v;
+  }
+};
+
+template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY>
+__global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ FgbLaunch L) {
+  using T = typename M::T;
+  constexpr int NF = Prog::kFields;
+  constexpr int R = Prog::kReach;
+  constexpr int H = K * R;
+  constexpr int P = 2 * R + 1;
+  constexpr int RY = TY + 2 * H, RX = TX + 2 * H;
+  constexpr int PL = NF * RY * RX;          // one plane of every field
+  extern __shared__ __align__(16) unsigned char fgb_smem_raw[];
+  T* rings = reinterpret_cast<T*>(fgb_smem_raw);   // [K][P][NF][RY][RX]
+  static_assert(Prog::kShift >= 0, "the per-step roll is non-negative");
+  const int nz = L.n[0], ny = L.n[1], nx = L.n[2];
+  const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
+  // the streamed axis is cut into gridDim.z chunks of planes [z0, z1)
+  const int zc = (nz + gridDim.z - 1) / gridDim.z;
+  const int z0 = blockIdx.z * zc, z1 = min(nz, z0 + zc);
+  if (z0 >= z1) return;
+  const T* __restrict__ U = static_cast<const T*>(L.uniforms);
+  const bool small = TY + H >= ny || TX + H >= nx || H >= nz || K * Prog::kShift >= nx ||
+                     K * Prog::kShift >= ny || K * Prog::kShift >= nz;
+
+  // input planes run over [z0 - H, z1 + H); level t works on plane zin - t*R
+  for (int zin = z0 - H; zin < z1 + H; ++zin) {
+    {  // level 0: load the plane (periodic in all axes)
+      const int gz = small ? pmod(zin, nz) : pwrap(zin, nz);
+      T* dst = rings + PlaneAccess<T, NF, P, RY, RX>::slot(zin) * PL;
+      for (int ly = threadIdx.y; ly < RY; ly += BY) {
+        const int gy = small ? pmod(y0 - H + ly, ny) : pwrap(y0 - H + ly, ny);
+        for (int lx = threadIdx.x; lx < RX; lx += BX) {
+          const int gx = small ? pmod(x0 - H + lx, nx) : pwrap(x0 - H + lx, nx);
+          const size_t g = ((size_t)gz * ny + gy) * nx + gx;
+#pragma unroll
+          for (int f = 0; f < NF; ++f)
+            dst[(f * RY + ly) * RX + lx] = Storage<S, T>::load(static_cast<const S*>(L.in[f])[g], L.scale[f]);
+        }
+      }
+    }
+    __syncthreads();
+#pragma unroll 1
+    for (int t = 1; t <= K; ++t) {
+      const int zt = zin - t * R;
+      if (zt < z0 - (K - t) * R) break;   // this level has nothing to compute yet
+      const T* below = rings + (size_t)(t - 1) * P * PL;
+      const int lo = t * R;
+      if (t < K) {
+        T* mine = rings + (size_t)t * P * PL + PlaneAccess<T, NF, P, RY, RX>::slot(zt) * PL;
+        for (int ly = lo + threadIdx.y; ly < RY - lo; ly += BY) {
+          for (int lx = lo + threadIdx.x; lx < RX - lo; lx += BX) {
+            T res[NF];
+            PlaneAccess<T, NF, P, RY, RX> a{below, zt, ly, lx, res};
+            Stage::template run<M>(a, U);
+#pragma unroll
+            for (int f = 0; f < NF; ++f) mine[(f * RY + ly) * RX + lx] = res[f];
+          }
+        }
+      } else {
+        // final level: the tile's cells of plane zt, straight to HBM
+        const int oz = small ? (zt + K * Prog::kShift) % nz : pwrap(zt + K * Prog::kShift, nz);
+        for (int ty = threadIdx.y; ty < TY; ty += BY) {
+          const int py = y0 + ty;
+          if (py >= ny) break;
+          const int oy = small ? (py + K * Prog::kShift) % ny : pwrap(py + K * Prog::kShift, ny);
+          for (int tx = threadIdx.x; tx < TX; tx += BX) {
+            const int px = x0 + tx;
+            if (px >= nx) break;
+            const int ox = small ? (px + K * Prog::kShift) % nx : pwrap(px + K * Prog::kShift, nx);
+            T res[NF];
+            PlaneAccess<T, NF, P, RY, RX> a{below, zt, ty + H, tx + H, res};
+            Stage::template run<M>(a, U);
+            const size_t g = ((size_t)oz * ny + oy) * nx + ox;
+#pragma unroll
+            for (int f = 0; f < NF; ++f)
+              static_cast<S*>(L.out[f])[g] = Storage<S, T>::store(res[f], L.inv_scale[f]);
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+template <class Prog, int P, class Stage, int TX, int TY, int K>
+struct Tb3dVariant {
+  using M = typename Precision<P>::M;
+  using S = typename Precision<P>::S;
+  using T = typename M::T;
+  static constexpr int BX = 32, BY = 8;
+  static constexpr int H = K * Prog::kReach;
+  static constexpr size_t kSmem =
+      (size_t)K * (2 * Prog::kReach + 1) * Prog::kFields * (TY + 2 * H) * (TX + 2 * H) * sizeof(T);
+
+  static cudaError_t launch(const FgbLaunch* L, cudaStream_t stream) {
+    auto kern = tb3d_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY>;
+    static bool configured = false;
+    if (!configured) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
+      if (e != cudaSuccess) return e;
+      configured = true;
+    }
+    // enough CTAs to fill the SMs several times over; each chunk re-reads
+    // 2H halo planes, so chunks stay at least 4H planes deep
+    const int gx = (L->n[2] + TX - 1) / TX, gy = (L->n[1] + TY - 1) / TY;
+    const int want = (1216 + gx * gy - 1) / (gx * gy);
+    const int most = L->n[0] / (4 * H) > 1 ? L->n[0] / (4 * H) : 1;
+    const int gz = want < most ? want : most;
+    kern<<<dim3(gx, gy, gz), dim3(BX, BY), kSmem, stream>>>(*L);
+    return cudaGetLastError();
+  }
+  static FgbFusedVariant describe() {
+    FgbFusedVariant v;
+    v.launch = &launch;
     v.tile_x = TX;
     v.tile_y = TY;
     v.steps = K;

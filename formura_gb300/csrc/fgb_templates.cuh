@@ -276,6 +276,18 @@ struct FusedFill {
       } else {
         d.nbatch[P] = 0;
       }
+    } else if constexpr (Prog::kDim == 3 && Prog::kStages == 1 && Prog::kMids == 0) {
+      const FgbFusedVariant v[] = {
+          Tb3dVariant<Prog, P, Stage0, 64, 16, 2>::describe(),
+          Tb3dVariant<Prog, P, Stage0, 64, 16, 4>::describe(),
+          Tb3dVariant<Prog, P, Stage0, 32, 32, 4>::describe(),
+          Tb3dVariant<Prog, P, Stage0, 64, 32, 4>::describe(),
+          Tb3dVariant<Prog, P, Stage0, 128, 16, 4>::describe(),
+          Tb3dVariant<Prog, P, Stage0, 32, 16, 8>::describe(),
+      };
+      d.nfused[P] = (int)(sizeof v / sizeof v[0]);
+      for (int i = 0; i < d.nfused[P]; ++i) d.fused[P][i] = v[i];
+      d.nbatch[P] = 0;
     } else {
       d.nfused[P] = 0;
       d.nbatch[P] = 0;

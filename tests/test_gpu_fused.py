@@ -74,3 +74,33 @@ def test_f16_fused_close_to_f32():
     fa, fb = a.download(), b.download()
     for i in range(2):
         assert W.rel_l2(fb[i], fa[i]) < 2e-2
+
+
+@pytest.mark.parametrize("shape", [(48, 48, 48), (40, 50, 70), (8, 40, 36), (96, 20, 130)])
+@pytest.mark.parametrize("prec", ["f64", "f32"])
+def test_3d_streaming_variants_match_single_steps(shape, prec):
+    """The 2.5D streaming kernels (K steps per launch, planes of the slowest
+    axis in a shared-memory ring) equal one step per launch bit for bit."""
+    src, _ = builtin_program("heat3d")
+    _, U = program_uniforms(src, W.heat_config(shape[2]), "heat3d")
+    x = np.random.default_rng(5).random((1,) + shape)
+    steps = 37
+    g = Grid("heat3d", shape, prec, U)
+    g.upload(x)
+    g.forward(steps)
+    ref = g.download()
+    variants = g.variants()
+    assert len(variants) >= 4
+    tried = 0
+    for v in variants:
+        g.upload(x)
+        try:
+            g.set_variant(v["index"])
+        except Exception:
+            continue            # does not fit this device's shared memory
+        tried += 1
+        g.forward(steps)
+        got = g.download()
+        assert np.array_equal(got, ref), v
+    assert tried >= 3
+    g.close()
