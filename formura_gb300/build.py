@@ -132,7 +132,7 @@ def build(names: Optional[List[str]] = None, jobs: Optional[int] = None, verbose
         raise RuntimeError("nvcc not found: the CUDA toolkit is required to build formura_gb300")
     gen = generate(names)
     os.makedirs(BUILD, exist_ok=True)
-    deps = [os.path.join(CSRC, f) for f in ("fgb_internal.h", "fgb_templates.cuh", "fgb_fused.cuh")
+    deps = [os.path.join(CSRC, f) for f in ("fgb_internal.h", "fgb_templates.cuh", "fgb_fused.cuh", "fgb_softf64.h")
             if os.path.exists(os.path.join(CSRC, f))] + [os.path.join(ROOT, "include", "formura_gb300.h")]
     units = [(os.path.join(CSRC, "fgb_runtime.cu"), os.path.join(BUILD, "fgb_runtime.o")),
              (os.path.join(CSRC, "fgb_noalloc.cu"), os.path.join(BUILD, "fgb_noalloc.o")),

@@ -9,6 +9,7 @@
 #include <stdint.h>
 #include <type_traits>
 #include "fgb_internal.h"
+#include "fgb_softf64.h"
 
 namespace fgb {
 
@@ -38,6 +39,50 @@ struct F64Exact {
     return __fma_rn(e, rc, q);
 #endif
   }
+  // The same operations on the integer pipes (fgb_softf64.h), with the
+  // hardware instruction for the operands outside the fast path: the
+  // generated code sends part of its adds, multiplies and power-of-two
+  // multiply-adds here so that both pipes work.  Bit-identical results.
+  // The hardware fallback sits behind a warp-uniform branch: a predicated
+  // FP64 instruction would still take its turn on the FP64 pipe.
+  static __device__ __forceinline__ T sadd(T a, T b) {
+    uint64_t r;
+    const bool ok = soft::add_bits(soft::to_bits(a), soft::to_bits(b), r);
+    T v = soft::from_bits(r);
+    if (__any_sync(__activemask(), !ok)) v = ok ? v : __dadd_rn(a, b);
+    return v;
+  }
+  static __device__ __forceinline__ T ssub(T a, T b) {
+    uint64_t r;
+    const bool ok = soft::add_bits(soft::to_bits(a), soft::to_bits(b) ^ soft::kSign, r);
+    T v = soft::from_bits(r);
+    if (__any_sync(__activemask(), !ok)) v = ok ? v : __dsub_rn(a, b);
+    return v;
+  }
+  static __device__ __forceinline__ T smul(T a, T b) {
+    uint64_t r;
+    const bool ok = soft::mul_bits(soft::to_bits(a), soft::to_bits(b), r);
+    T v = soft::from_bits(r);
+    if (__any_sync(__activemask(), !ok)) v = ok ? v : __dmul_rn(a, b);
+    return v;
+  }
+  static __device__ __forceinline__ T sfma(T c, T h, T t) {
+    uint64_t r;
+    const bool ok = soft::scaled_add_bits(soft::to_bits(c), soft::to_bits(h), soft::to_bits(t), r);
+    T v = soft::from_bits(r);
+    if (__any_sync(__activemask(), !ok)) v = ok ? v : __fma_rn(c, h, t);
+    return v;
+  }
+  // Markstein quotient with its first product on the integer pipes
+  static __device__ __forceinline__ T sdivu(T x, T c, T rc) {
+#ifdef FGB_DIVU_IEEE
+    (void)rc;
+    return __ddiv_rn(x, c);
+#endif
+    const T q = smul(x, rc);
+    const T e = __fma_rn(-q, c, x);
+    return __fma_rn(e, rc, q);
+  }
   static __device__ __forceinline__ T neg(T a) { return -a; }
   static __device__ __forceinline__ T sqrt(T a) { return __dsqrt_rn(a); }
   static __device__ __forceinline__ T fabs(T a) { return ::fabs(a); }
@@ -57,6 +102,11 @@ struct F64Fast {
   static __device__ __forceinline__ T div(T a, T b) { return a / b; }
   static __device__ __forceinline__ T fma(T a, T b, T c) { return ::fma(a, b, c); }
   static __device__ __forceinline__ T divu(T x, T, T rc) { return x * rc; }
+  static __device__ __forceinline__ T sadd(T a, T b) { return a + b; }
+  static __device__ __forceinline__ T ssub(T a, T b) { return a - b; }
+  static __device__ __forceinline__ T smul(T a, T b) { return a * b; }
+  static __device__ __forceinline__ T sfma(T a, T b, T c) { return ::fma(a, b, c); }
+  static __device__ __forceinline__ T sdivu(T x, T, T rc) { return x * rc; }
   static __device__ __forceinline__ T neg(T a) { return -a; }
   static __device__ __forceinline__ T sqrt(T a) { return ::sqrt(a); }
   static __device__ __forceinline__ T fabs(T a) { return ::fabs(a); }
@@ -76,6 +126,11 @@ struct F32 {
   static __device__ __forceinline__ T div(T a, T b) { return a / b; }
   static __device__ __forceinline__ T fma(T a, T b, T c) { return fmaf(a, b, c); }
   static __device__ __forceinline__ T divu(T x, T, T rc) { return x * rc; }
+  static __device__ __forceinline__ T sadd(T a, T b) { return a + b; }
+  static __device__ __forceinline__ T ssub(T a, T b) { return a - b; }
+  static __device__ __forceinline__ T smul(T a, T b) { return a * b; }
+  static __device__ __forceinline__ T sfma(T a, T b, T c) { return fmaf(a, b, c); }
+  static __device__ __forceinline__ T sdivu(T x, T, T rc) { return x * rc; }
   static __device__ __forceinline__ T neg(T a) { return -a; }
   static __device__ __forceinline__ T sqrt(T a) { return sqrtf(a); }
   static __device__ __forceinline__ T fabs(T a) { return fabsf(a); }
@@ -129,6 +184,29 @@ __device__ __forceinline__ int wrap(int p, int n) {
   }
 }
 
+// periodic wrap for offsets up to twice the axis length (adjoint cursors
+// combine the stencil reach with the roll)
+template <int D>
+__device__ __forceinline__ int wrap2(int p, int n) {
+  if constexpr (D >= -1 && D <= 1) {
+    return wrap<D>(p, n);
+  } else if constexpr (D > 0) {
+    int i = p + D;
+    i = i >= n ? i - n : i;
+    return i >= n ? i - n : i;
+  } else {
+    int i = p + D;
+    i = i < 0 ? i + n : i;
+    return i < 0 ? i + n : i;
+  }
+}
+
+// Every buffer a kernel reads is read-only for that launch (the stages of a
+// step write only arrays that later launches read), so loads go through the
+// non-coherent path and may be scheduled ahead of the launch's stores.
+template <class X>
+__device__ __forceinline__ X ro_load(const X* p) { return __ldg(p); }
+
 // Accessor of the generic stage kernel: global loads at p + D, stores of the
 // new state at p + shift (the reference's per-step roll, Templates.hs:346).
 template <class S, class T, int DIM, int SHIFT>
@@ -143,12 +221,12 @@ struct GlobalAccess {
   __device__ __forceinline__ T ld() const {
     const S* a = static_cast<const S*>(L.in[F]);
     const uint32_t k = lin(wrap<D0>(p0, L.n[0]), wrap<D1>(p1, L.n[1]), wrap<D2>(p2, L.n[2]));
-    return Storage<S, T>::load(a[k], L.scale[F]);
+    return Storage<S, T>::load(ro_load(a + k), L.scale[F]);
   }
   template <int K, int D0, int D1, int D2>
   __device__ __forceinline__ T ldm() const {
     const T* a = static_cast<const T*>(L.mid[K]);
-    return a[lin(wrap<D0>(p0, L.n[0]), wrap<D1>(p1, L.n[1]), wrap<D2>(p2, L.n[2]))];
+    return ro_load(a + lin(wrap<D0>(p0, L.n[0]), wrap<D1>(p1, L.n[1]), wrap<D2>(p2, L.n[2])));
   }
   template <int F>
   __device__ __forceinline__ void st(T v) const {
@@ -176,23 +254,17 @@ struct AdjointAccess {
   __device__ __forceinline__ uint32_t lin(int i0, int i1, int i2) const {
     return ((uint32_t)i0 * (uint32_t)L.n[1] + (uint32_t)i1) * (uint32_t)L.n[2] + (uint32_t)i2;
   }
-  __device__ __forceinline__ static int wrapv(int p, int d, int n) {
-    int i = p + d;
-    while (i < 0) i += n;
-    while (i >= n) i -= n;
-    return i;
-  }
   template <int F, int D0, int D1, int D2>
   __device__ __forceinline__ T ld() const {
     const S* a = static_cast<const S*>(L.in[F]);
-    return Storage<S, T>::load(a[lin(wrapv(p0, D0, L.n[0]), wrapv(p1, D1, L.n[1]), wrapv(p2, D2, L.n[2]))],
-                               L.scale[F]);
+    return Storage<S, T>::load(
+        ro_load(a + lin(wrap2<D0>(p0, L.n[0]), wrap2<D1>(p1, L.n[1]), wrap2<D2>(p2, L.n[2]))), L.scale[F]);
   }
   template <int F, int D0, int D1, int D2>
   __device__ __forceinline__ T ldl() const {
     const S* a = static_cast<const S*>(L.mid[F]);
-    return Storage<S, T>::load(a[lin(wrapv(p0, D0, L.n[0]), wrapv(p1, D1, L.n[1]), wrapv(p2, D2, L.n[2]))],
-                               1.0f);
+    return Storage<S, T>::load(
+        ro_load(a + lin(wrap2<D0>(p0, L.n[0]), wrap2<D1>(p1, L.n[1]), wrap2<D2>(p2, L.n[2]))), 1.0f);
   }
   template <int F>
   __device__ __forceinline__ void stl(T v) const {
@@ -202,30 +274,50 @@ struct AdjointAccess {
 
 constexpr int kBlockX = 128;
 
-// One thread per grid point; x covers the contiguous (last) axis.
-template <class M, class S, int DIM, int SHIFT, class Stage>
+// One thread per grid point of RPT consecutive rows (the middle axis); x
+// covers the contiguous (last) axis.  With RPT > 1 a thread has the loads of
+// several points in flight at once, which is what a memory-bound FP32/FP16
+// step needs to cover the HBM latency.
+template <class M, class S, int DIM, int SHIFT, class Stage, int RPT>
 __global__ void __launch_bounds__(kBlockX) stage_kernel(const __grid_constant__ FgbLaunch L) {
   const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
   if (p2 >= L.n[2]) return;
-  GlobalAccess<S, typename M::T, DIM, SHIFT> a{L, (int)blockIdx.z, (int)blockIdx.y, p2};
-  Stage::template run<M>(a, static_cast<const typename M::T*>(L.uniforms));
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) {
+    const int p1 = (int)blockIdx.y * RPT + r;
+    if (RPT > 1 && p1 >= L.n[1]) break;
+    GlobalAccess<S, typename M::T, DIM, SHIFT> a{L, (int)blockIdx.z, p1, p2};
+    Stage::template run<M>(a, static_cast<const typename M::T*>(L.uniforms));
+  }
 }
 
-template <class M, class S, class Adj>
+template <class M, class S, class Adj, int RPT>
 __global__ void __launch_bounds__(kBlockX) adjoint_kernel(const __grid_constant__ FgbLaunch L) {
   const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
   if (p2 >= L.n[2]) return;
-  AdjointAccess<S, typename M::T> a{L, (int)blockIdx.z, (int)blockIdx.y, p2};
-  Adj::template run<M>(a, static_cast<const typename M::T*>(L.uniforms));
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) {
+    const int p1 = (int)blockIdx.y * RPT + r;
+    if (RPT > 1 && p1 >= L.n[1]) break;
+    AdjointAccess<S, typename M::T> a{L, (int)blockIdx.z, p1, p2};
+    Adj::template run<M>(a, static_cast<const typename M::T*>(L.uniforms));
+  }
 }
+
+// rows per thread: several for the memory-bound FP32/FP16 forms of
+// single-kernel steps, one for FP64 (bound by the FP64 pipe) and for the
+// register-heavy stages of multi-stage programs
+template <int P, bool Light>
+constexpr int rows_per_thread() { return (P >= 2 && Light) ? 4 : 1; }
 
 template <int P, class Adj>
 cudaError_t launch_adjoint(const FgbLaunch* L, cudaStream_t stream) {
   using M = typename Precision<P>::M;
   using S = typename Precision<P>::S;
+  constexpr int R = rows_per_thread<P, true>();
   const int bx = L->n[2] >= kBlockX ? kBlockX : ((L->n[2] + 31) / 32) * 32;
-  dim3 grid((L->n[2] + bx - 1) / bx, L->n[1], L->n[0]);
-  adjoint_kernel<M, S, Adj><<<grid, bx, 0, stream>>>(*L);
+  dim3 grid((L->n[2] + bx - 1) / bx, (L->n[1] + R - 1) / R, L->n[0]);
+  adjoint_kernel<M, S, Adj, R><<<grid, bx, 0, stream>>>(*L);
   return cudaGetLastError();
 }
 
@@ -233,9 +325,10 @@ template <class Prog, int P, class Stage>
 cudaError_t launch_stage(const FgbLaunch* L, cudaStream_t stream) {
   using M = typename Precision<P>::M;
   using S = typename Precision<P>::S;
+  constexpr int R = rows_per_thread<P, Prog::kStages == 1 && Prog::kMids == 0>();
   const int bx = L->n[2] >= kBlockX ? kBlockX : ((L->n[2] + 31) / 32) * 32;
-  dim3 grid((L->n[2] + bx - 1) / bx, L->n[1], L->n[0]);
-  stage_kernel<M, S, Prog::kDim, Prog::kShift, Stage><<<grid, bx, 0, stream>>>(*L);
+  dim3 grid((L->n[2] + bx - 1) / bx, (L->n[1] + R - 1) / R, L->n[0]);
+  stage_kernel<M, S, Prog::kDim, Prog::kShift, Stage, R><<<grid, bx, 0, stream>>>(*L);
   return cudaGetLastError();
 }
 

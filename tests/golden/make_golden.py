@@ -9,7 +9,12 @@ programs, run through the restated Formura generator (the oracle):
 
 Each fixture stores the seeded input state, the config, the step count and
 the output state and grid offset.  The shipped programs (heat3d, gs2d,
-hllc3d, hlld3d) must reproduce them bit for bit.  Needs the reference tree; run from
+hllc3d, hlld3d) must reproduce them bit for bit.
+
+A fifth fixture, sod1d_t100, holds the exact Riemann solution table of
+sample/1d_hllc (ref_data/exact.dat: x, rho, u, p, e at step 100) and the
+primitive profile of that sample's own program after 100 steps through the
+oracle, the accuracy a shock-tube run of the shipped sod1d program is held to.  Needs the reference tree; run from
 the repository root:  python tests/golden/make_golden.py
 """
 import os
@@ -51,6 +56,23 @@ def make(name, src, cfg, steps, state_fn, field_map):
     print("wrote", name)
 
 
+def make_sod(name="sod1d_t100", steps=100):
+    exact = np.loadtxt(os.path.join(REF, "sample/1d_hllc/ref_data/exact.dat"))
+    ref = ReferenceProgram(reference_source("sample/1d_hllc/hllc.fmr"),
+                           reference_source("sample/1d_hllc/config.yaml"), "mkgold_sod")
+    ref.init()
+    nav = ref.forward(steps)
+    rho = ref.get("rho")
+    u = ref.get("rhou") / rho
+    ek = 0.5 * rho * (u * u + (ref.get("rhov") / rho) ** 2 + (ref.get("rhow") / rho) ** 2)
+    p = 0.4 * (ref.get("e") - ek)
+    x = np.array([ref.to_pos("x", i) for i in range(rho.size)])
+    np.savez_compressed(os.path.join(OUT, name + ".npz"), exact_x=exact[:, 0], exact_rho=exact[:, 1],
+                        exact_u=exact[:, 2], exact_p=exact[:, 3], sample_x=x, sample_rho=rho, sample_u=u,
+                        sample_p=p, steps=steps, time_step=nav["time_step"])
+    print("wrote", name)
+
+
 if __name__ == "__main__":
     make("heat3d_16_10", reference_source("examples/diffusion3/diffusion3.fmr"), W.heat_config(16), 10,
          lambda r: W.heat_state((16, 16, 16), 11), {"q": "q"})
@@ -66,3 +88,4 @@ if __name__ == "__main__":
          lambda r: W.mhd_state((12, 12, 12), 14),
          {"bx": "B_x", "by": "B_y", "bz": "B_z", "e": "e", "mx": "rhou", "my": "rhov", "mz": "rhow",
           "psi": "psi", "rho": "rho"})
+    make_sod()

@@ -233,3 +233,40 @@ def test_hllc_conserved_totals_fp64(prec):
     drift = np.abs(t1 - t0) / scale
     assert (drift < (1e-13 if prec == "f64" else 1e-5)).all(), drift
     g.close()
+
+
+def _sod_profile(p):
+    rho = p.get("rho")
+    u = p.get("m") / rho
+    pr = 0.4 * (p.get("e") - 0.5 * rho * u * u)
+    x = np.array([p.to_pos("x", i) for i in range(rho.size)])
+    return x, rho, u, pr
+
+
+def test_sod_shock_tube_bit_exact_and_accurate():
+    """1D shock tube, 400 cells, 100 steps through the drop-in: bit-identical
+    to the oracle, and as close to the exact Riemann solution of the
+    reference's 1D HLLC sample (L1 over the waves) as that sample's own
+    program is."""
+    import os
+    src, cfg = builtin_program("sod1d")
+    ref, gpu = _pair("sod1d", cfg, "", "sod")
+    _check_navi(ref.init(), gpu.init())
+    for f in ("e", "m", "rho"):
+        assert np.array_equal(ref.get(f), gpu.get(f))
+    ref.forward(100)
+    for _ in range(100):
+        gpu.forward(1)
+    _check_navi(ref.navi_dict(), gpu.navi_dict())
+    for f in ("e", "m", "rho"):
+        assert np.array_equal(ref.get(f), gpu.get(f)), f
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "sod1d_t100.npz"))
+    x, rho, u, pr = _sod_profile(gpu)
+    sel = (x > 1.2) & (x < 2.8)
+    for name, v in (("rho", rho), ("u", u), ("p", pr)):
+        err = np.mean(np.abs(v[sel] - np.interp(x[sel], d["exact_x"], d["exact_" + name])))
+        xs = d["sample_x"]
+        ss = (xs > 1.2) & (xs < 2.8)
+        err_sample = np.mean(np.abs(d["sample_" + name][ss] - np.interp(xs[ss], d["exact_x"], d["exact_" + name])))
+        assert err <= 1.01 * err_sample + 1e-12, (name, err, err_sample)
+    gpu.finalize()

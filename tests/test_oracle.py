@@ -157,3 +157,29 @@ def test_reference_samples_compile():
         assert len(mm.step) == nman
         if fields:
             assert mm.fields == fields
+
+
+def test_sod_shock_tube_oracle_matches_exact_solution():
+    """Physics pin of the oracle: the shipped 1D shock-tube program, run 100
+    steps through the restated generator, against the exact Riemann solution
+    table of the reference's 1D HLLC sample (tests/golden/sod1d_t100.npz).
+    Its L1 error over the waves equals that of the sample's own program."""
+    from formura_gb300.host import builtin_program
+    src, cfg = builtin_program("sod1d")
+    d = np.load(os.path.join(os.path.dirname(__file__), "golden", "sod1d_t100.npz"))
+    r = ReferenceProgram(src, cfg, "sod_oracle")
+    r.init()
+    nav = r.forward(100)
+    assert nav["time_step"] == int(d["time_step"]) == 100
+    rho = r.get("rho")
+    u = r.get("m") / rho
+    p = 0.4 * (r.get("e") - 0.5 * rho * u * u)
+    x = np.array([r.to_pos("x", i) for i in range(rho.size)])
+    sel = (x > 1.2) & (x < 2.8)
+    xs = d["sample_x"]
+    ss = (xs > 1.2) & (xs < 2.8)
+    for name, v in (("rho", rho), ("u", u), ("p", p)):
+        err = np.mean(np.abs(v[sel] - np.interp(x[sel], d["exact_x"], d["exact_" + name])))
+        err_sample = np.mean(np.abs(d["sample_" + name][ss] - np.interp(xs[ss], d["exact_x"], d["exact_" + name])))
+        assert err < 0.01 and err <= 1.01 * err_sample + 1e-12, (name, err, err_sample)
+
