@@ -204,6 +204,27 @@ def load_traffic(spec, precision, variant=-1):
     return d.get(key)
 
 
+def fp64_pipe(spec, precision, value):
+    """The bound of the bit-exact FP64 kernels: FP64-pipe instructions per
+    lattice update (ncu sm__inst_executed_pipe_fp64 / updates, from
+    profiles/fp64_pipe.json) times the update rate, against the measured DFMA
+    rate of this part (profiles/gb300_fp_throughput_probe.md)."""
+    if precision != "f64":
+        return None
+    p = os.path.join(ROOT, "profiles", "fp64_pipe.json")
+    if not os.path.exists(p):
+        return None
+    with open(p) as f:
+        d = json.load(f)
+    per = d.get("per_update", {}).get(spec["program"])
+    if per is None:
+        return None
+    peak = float(d["peak_ginst_per_s"])
+    achieved = value * per
+    return {"instructions_per_update": per, "achieved_ginst_per_s": achieved, "peak_ginst_per_s": peak,
+            "frac": achieved / peak, "peak_source": d["peak_source"]}
+
+
 def storage_bytes(precision):
     return {"f64": 8, "f64fast": 8, "f32": 4, "f16": 2}[precision]
 
@@ -387,6 +408,9 @@ def run_ours(args, spec):
                                  (nf * cells * storage_bytes(args.precision) // 2**20),
                            "parallelism": "replicas" if ws > 1 else "single GPU"},
                 "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
+        fp64 = fp64_pipe(spec, args.precision, value / ws)
+        if fp64 is not None:
+            line["fp64_pipe_bound"] = fp64
         if cpu is not None:
             line["cpu_baseline"] = cpu
         if variants:

@@ -61,6 +61,25 @@ struct FgbBatchVariant {
   size_t smem_bytes;
 };
 
+// Adjoint of a multi-stage step (two passes per stage, see the generator's
+// adjoint.py): u and mid are the forward state u_n and the step's forward
+// arrays; lnext / lprev the adjoint of the new and of the old state (storage
+// type); lmid the adjoints of the forward arrays and pair the per-point
+// partial sums of one stage (compute type).
+#define FGB_MAX_PAIRS 256
+struct FgbAdjLaunch {
+  const void* u[FGB_MAX_FIELDS];
+  const void* mid[FGB_MAX_MIDS];
+  const void* lnext[FGB_MAX_FIELDS];
+  void* lprev[FGB_MAX_FIELDS];
+  void* lmid[FGB_MAX_MIDS];
+  void* pair[FGB_MAX_PAIRS];
+  const void* uniforms;
+  float scale[FGB_MAX_FIELDS];
+  int n[3];
+};
+typedef cudaError_t (*FgbAdjLaunchFn)(const FgbAdjLaunch* args, cudaStream_t stream);
+
 struct FgbProgramDesc {
   const char* name;
   int dim, nfields, nmids, nstages, sleeve, shift, reach, nuniforms;
@@ -73,6 +92,11 @@ struct FgbProgramDesc {
   FgbStageLaunch adjoint[FGB_NUM_PRECISIONS];
   FgbBatchVariant batch[FGB_NUM_PRECISIONS][FGB_MAX_FUSED];
   int nbatch[FGB_NUM_PRECISIONS];
+  // Adjoint of a multi-stage step: per stage, the partial-sum pass and the
+  // gather pass, and the number of (input array, cursor) pairs it reads.
+  FgbAdjLaunchFn adj_partial[FGB_NUM_PRECISIONS][FGB_MAX_STAGES];
+  FgbAdjLaunchFn adj_gather[FGB_NUM_PRECISIONS][FGB_MAX_STAGES];
+  int adj_pairs[FGB_MAX_STAGES];
 };
 
 typedef const FgbProgramDesc* (*FgbProgramGetter)(void);

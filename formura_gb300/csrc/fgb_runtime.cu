@@ -117,6 +117,8 @@ struct fgb_grid {
   // reverse mode
   void* lam[2] = {nullptr, nullptr};    // adjoint state, storage precision
   int lcur = 0;
+  void* lam_mids = nullptr;             // multi-stage adjoint: adjoints of the forward arrays
+  void* pairs = nullptr;                // and the partial sums of one stage (compute type)
   std::vector<void*> snaps;             // checkpoints of the forward state
   int grad_steps = -1;                  // steps recorded by fgb_gradient_forward
   int64_t grad_fwd = 0, grad_adj = 0;   // forward steps (incl. recomputation) and adjoint steps
@@ -269,6 +271,8 @@ int fgb_close(fgb_grid* g) {
   cudaFree(g->staging);
   cudaFree(g->lam[0]);
   cudaFree(g->lam[1]);
+  cudaFree(g->lam_mids);
+  cudaFree(g->pairs);
   for (auto& sb : g->sub) {
     cudaFree(sb.uniforms);
     cudaFree(sb.mids);
@@ -460,11 +464,23 @@ int fgb_autotune(fgb_grid* g, int trial_steps, int* chosen) {
 // ---------------------------------------------------------------------------
 static size_t state_bytes(const fgb_grid* g) { return g->cells * g->prog->nfields * storage_size(g->precision); }
 
+static bool stage_adjoint(const fgb_grid* g) {
+  return g->prog->nstages > 1 && g->prog->adj_partial[g->precision][0] != nullptr;
+}
+
 static int ensure_adjoint(fgb_grid* g) {
-  if (!g->prog->adjoint[g->precision])
+  if (!g->prog->adjoint[g->precision] && !stage_adjoint(g))
     return fail(FGB_E_ARG, "program %s has no adjoint in this precision", g->prog->name);
   for (int b = 0; b < 2; ++b)
     if (!g->lam[b]) FGB_CUDA(cudaMalloc(&g->lam[b], state_bytes(g)), "adjoint state");
+  if (stage_adjoint(g)) {
+    const size_t cs = compute_size(g->precision);
+    int most = 0;
+    for (int s = 0; s < g->prog->nstages; ++s) most = std::max(most, g->prog->adj_pairs[s]);
+    if (!g->lam_mids && g->prog->nmids > 0)
+      FGB_CUDA(cudaMalloc(&g->lam_mids, g->cells * g->prog->nmids * cs), "adjoint of the forward arrays");
+    if (!g->pairs && most > 0) FGB_CUDA(cudaMalloc(&g->pairs, g->cells * most * cs), "adjoint partial sums");
+  }
   return FGB_OK;
 }
 
@@ -498,8 +514,50 @@ static int state_to_host(fgb_grid* g, const void* src, double* host) {
   return FGB_OK;
 }
 
+// Multi-stage step: recompute the step's forward arrays from u, then run the
+// two adjoint passes of each stage from the last stage to the first.
+static int stage_adjoint_step(fgb_grid* g, const void* u) {
+  const FgbProgramDesc* d = g->prog;
+  const size_t es = storage_size(g->precision), cs = compute_size(g->precision);
+  FgbLaunch L;
+  fill_launch(g, g->cur, &L);
+  for (int f = 0; f < d->nfields; ++f) L.in[f] = (const char*)u + f * g->cells * es;
+  for (int st = 0; st + 1 < d->nstages; ++st) {
+    cudaError_t e = d->launch[g->precision][st](&L, g->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "stage launch");
+    ++g->launches;
+  }
+  FgbAdjLaunch A;
+  memset(&A, 0, sizeof A);
+  for (int f = 0; f < d->nfields; ++f) {
+    A.u[f] = (const char*)u + f * g->cells * es;
+    A.lnext[f] = (const char*)g->lam[g->lcur] + f * g->cells * es;
+    A.lprev[f] = (char*)g->lam[g->lcur ^ 1] + f * g->cells * es;
+    A.scale[f] = g->scale[f];
+  }
+  for (int k = 0; k < d->nmids; ++k) {
+    A.mid[k] = (const char*)g->mids + k * g->cells * cs;
+    A.lmid[k] = (char*)g->lam_mids + k * g->cells * cs;
+  }
+  for (int s = 0; s < d->nstages; ++s)
+    if (d->adj_pairs[s] > FGB_MAX_PAIRS) return fail(FGB_E_ARG, "stage %d reads too many arrays", s);
+  A.uniforms = g->uniforms;
+  for (int a = 0; a < 3; ++a) A.n[a] = g->n[a];
+  for (int s = d->nstages - 1; s >= 0; --s) {
+    for (int j = 0; j < d->adj_pairs[s]; ++j) A.pair[j] = (char*)g->pairs + (size_t)j * g->cells * cs;
+    cudaError_t e = d->adj_partial[g->precision][s](&A, g->stream);
+    if (e == cudaSuccess) e = d->adj_gather[g->precision][s](&A, g->stream);
+    if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
+    g->launches += 2;
+  }
+  ++g->grad_adj;
+  g->lcur ^= 1;
+  return FGB_OK;
+}
+
 // lambda <- (dF/du at `u`)^T lambda
 static int adjoint_step(fgb_grid* g, const void* u) {
+  if (!g->prog->adjoint[g->precision]) return stage_adjoint_step(g, u);
   FgbLaunch L;
   fill_launch(g, g->cur, &L);
   const size_t es = storage_size(g->precision);

@@ -402,6 +402,134 @@ struct AdjointFill {
   }
 };
 
+// ---------------------------------------------------------------------------
+// adjoint of multi-stage steps
+// ---------------------------------------------------------------------------
+// Partial-sum pass: the stage's forward at p (its stores are dropped), the
+// adjoints of its outputs at p, and one partial sum per (input, cursor).
+template <class S, class T, int DIM, int SHIFT>
+struct AdjPartialAccess {
+  const FgbAdjLaunch& L;
+  int p0, p1, p2;
+  __device__ __forceinline__ uint32_t lin(int i0, int i1, int i2) const {
+    return ((uint32_t)i0 * (uint32_t)L.n[1] + (uint32_t)i1) * (uint32_t)L.n[2] + (uint32_t)i2;
+  }
+  template <int D0, int D1, int D2>
+  __device__ __forceinline__ uint32_t at() const {
+    return lin(wrap2<D0>(p0, L.n[0]), wrap2<D1>(p1, L.n[1]), wrap2<D2>(p2, L.n[2]));
+  }
+  template <int F, int D0, int D1, int D2>
+  __device__ __forceinline__ T ld() const {
+    return Storage<S, T>::load(ro_load(static_cast<const S*>(L.u[F]) + at<D0, D1, D2>()), L.scale[F]);
+  }
+  template <int K, int D0, int D1, int D2>
+  __device__ __forceinline__ T ldm() const {
+    return ro_load(static_cast<const T*>(L.mid[K]) + at<D0, D1, D2>());
+  }
+  template <int F>
+  __device__ __forceinline__ void st(T) const {}
+  template <int K>
+  __device__ __forceinline__ void stm(T) const {}
+  template <int F, int D0, int D1, int D2>
+  __device__ __forceinline__ T ldl() const {
+    return Storage<S, T>::load(ro_load(static_cast<const S*>(L.lnext[F]) + at<D0, D1, D2>()), 1.0f);
+  }
+  template <int K>
+  __device__ __forceinline__ T ldlm() const {
+    return ro_load(static_cast<const T*>(L.lmid[K]) + lin(p0, p1, p2));
+  }
+  template <int J>
+  __device__ __forceinline__ void stp(T v) const {
+    static_cast<T*>(L.pair[J])[lin(p0, p1, p2)] = v;
+  }
+};
+
+// Gather pass: lambda of each input array at q from the partial sums at q - c.
+template <class S, class T>
+struct AdjGatherAccess {
+  const FgbAdjLaunch& L;
+  int p0, p1, p2;
+  __device__ __forceinline__ uint32_t lin(int i0, int i1, int i2) const {
+    return ((uint32_t)i0 * (uint32_t)L.n[1] + (uint32_t)i1) * (uint32_t)L.n[2] + (uint32_t)i2;
+  }
+  template <int J, int D0, int D1, int D2>
+  __device__ __forceinline__ T ldp() const {
+    return ro_load(static_cast<const T*>(L.pair[J]) +
+                   lin(wrap2<D0>(p0, L.n[0]), wrap2<D1>(p1, L.n[1]), wrap2<D2>(p2, L.n[2])));
+  }
+  template <int G, bool FIRST>
+  __device__ __forceinline__ void accs(T v) const {
+    S* a = static_cast<S*>(L.lprev[G]) + lin(p0, p1, p2);
+    if (!FIRST) v = v + Storage<S, T>::load(*a, 1.0f);
+    *a = Storage<S, T>::store(v, 1.0f);
+  }
+  template <int K, bool FIRST>
+  __device__ __forceinline__ void accm(T v) const {
+    T* a = static_cast<T*>(L.lmid[K]) + lin(p0, p1, p2);
+    if (!FIRST) v = v + *a;
+    *a = v;
+  }
+};
+
+template <class M, class Acc, class F>
+__global__ void __launch_bounds__(kBlockX) adj_stage_kernel(const __grid_constant__ FgbAdjLaunch L) {
+  const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
+  if (p2 >= L.n[2]) return;
+  Acc a{L, (int)blockIdx.z, (int)blockIdx.y, p2};
+  F::template run<M>(a, static_cast<const typename M::T*>(L.uniforms));
+}
+
+template <class Prog, int P, class F, bool Gather>
+cudaError_t launch_adj_stage(const FgbAdjLaunch* L, cudaStream_t stream) {
+  using M = typename Precision<P>::M;
+  using S = typename Precision<P>::S;
+  using T = typename M::T;
+  using Acc = typename std::conditional<Gather, AdjGatherAccess<S, T>,
+                                        AdjPartialAccess<S, T, Prog::kDim, Prog::kShift>>::type;
+  const int bx = L->n[2] >= kBlockX ? kBlockX : ((L->n[2] + 31) / 32) * 32;
+  dim3 grid((L->n[2] + bx - 1) / bx, L->n[1], L->n[0]);
+  adj_stage_kernel<M, Acc, F><<<grid, bx, 0, stream>>>(*L);
+  return cudaGetLastError();
+}
+
+template <class Partial, class Gather>
+struct AdjointStagePair {
+  using P1 = Partial;
+  using P2 = Gather;
+};
+template <class... Pairs>
+struct AdjointStages {};
+
+template <class Prog, class A>
+struct StageAdjointFill {
+  static void fill(FgbProgramDesc& d) {
+    for (int p = 0; p < FGB_NUM_PRECISIONS; ++p)
+      for (int s = 0; s < FGB_MAX_STAGES; ++s) d.adj_partial[p][s] = d.adj_gather[p][s] = nullptr;
+  }
+};
+// FP64 (exact rounding) and FP32 forms; the others have no adjoint
+template <class Prog, class... Pairs>
+struct StageAdjointFill<Prog, AdjointStages<Pairs...>> {
+  static void fill(FgbProgramDesc& d) {
+    static_assert(sizeof...(Pairs) == Prog::kStages, "one adjoint pair per stage");
+    const int pairs[] = {Pairs::P1::kPairs...};
+    const FgbAdjLaunchFn p0[] = {&launch_adj_stage<Prog, 0, typename Pairs::P1, false>...};
+    const FgbAdjLaunchFn g0[] = {&launch_adj_stage<Prog, 0, typename Pairs::P2, true>...};
+    const FgbAdjLaunchFn p2[] = {&launch_adj_stage<Prog, 2, typename Pairs::P1, false>...};
+    const FgbAdjLaunchFn g2[] = {&launch_adj_stage<Prog, 2, typename Pairs::P2, true>...};
+    for (int p = 0; p < FGB_NUM_PRECISIONS; ++p)
+      for (int s = 0; s < FGB_MAX_STAGES; ++s) d.adj_partial[p][s] = d.adj_gather[p][s] = nullptr;
+    static_assert(((Pairs::P1::kPairs <= FGB_MAX_PAIRS) && ...), "too many (array, cursor) pairs in a stage");
+    for (int s = 0; s < (int)sizeof...(Pairs); ++s) {
+      d.adj_pairs[s] = pairs[s];
+      d.adj_partial[0][s] = p0[s];
+      d.adj_gather[0][s] = g0[s];
+      d.adj_partial[2][s] = p2[s];
+      d.adj_gather[2][s] = g2[s];
+    }
+  }
+};
+
 template <class Prog, class... Stages>
 struct ProgramBuilder {
   template <int P>
@@ -434,6 +562,7 @@ struct ProgramBuilder {
     FusedFill<Prog, Stages...>::template fill<2>(d);
     FusedFill<Prog, Stages...>::template fill<3>(d);
     AdjointFill<typename Prog::Adjoint>::fill(d);
+    StageAdjointFill<Prog, typename Prog::StageAdjoint>::fill(d);
     return d;
   }
 };

@@ -121,7 +121,7 @@ class _Algebra:
 
 
 def emit_adjoint(mm: MMProgram, name: str, pe: _ProgramEmitter = None):
-    """(CUDA source of ``struct Adjoint``, program emitter holding its table).
+    """(CUDA source of ``struct AdjointStep``, program emitter holding its table).
     Pass the forward program's emitter so that both share one uniform table."""
     pe = pe or _ProgramEmitter(mm, name, [])
     if len(pe.stages) != 1 or pe.mids:
@@ -258,7 +258,196 @@ def emit_adjoint(mm: MMProgram, name: str, pe: _ProgramEmitter = None):
             expr = f"M::add({expr}, {t})"
         out.append(f"    a.template stl<{g}>({expr});")
     body = "\n".join("    " + l.strip() for l in lines) + "\n" + "\n".join(out)
-    return (f"struct Adjoint {{\n"
+    return (f"struct AdjointStep {{\n"
             f"  template <class M, class A>\n"
             f"  static __device__ __forceinline__ void run(const A& a, const typename M::T* __restrict__ U) {{\n"
             f"    using T = typename M::T;\n    (void)U;\n{body}\n  }}\n}};\n"), pe
+
+
+# ---------------------------------------------------------------------------
+# multi-stage steps
+# ---------------------------------------------------------------------------
+def _as_alg(h):
+    """Forward handle of the stage emitter in the form _Algebra expects."""
+    if h[0] == "lit":
+        return ("u", ("lit", float(h[1])))
+    if h[0] == "u":
+        return ("u", h[1])
+    return h
+
+
+def emit_stage_adjoints(pe: _ProgramEmitter):
+    """Adjoint of a step made of several stages (HLLC, HLLD), as two functors
+    per stage.
+
+    Stage s computes its outputs o (manifest arrays, or the new state) at p
+    from its inputs x (state fields and earlier arrays) read at p + c.  With
+    lam_o the adjoint of each output:
+
+    * ``AdjStage<s>`` evaluates the stage forward at p once, seeds the reverse
+      sweep of its SSA chain with lam_o(p) (lam of the new state is read at
+      p + shift, where the forward wrote it) and stores, for every input read
+      (x, c), the partial sum P_(x,c)(p) = sum_o lam_o(p) * do(p)/dx(p + c);
+    * ``AdjGather<s>`` forms lam_x(q) = sum_c P_(x,c)(q - c) in a fixed order,
+      storing it for the first stage (in reverse order) that reads x and
+      adding to it for the others.
+
+    Stages run from last to first, after the forward arrays of the step were
+    recomputed from u_n.  Nothing is atomic, so the result is deterministic.
+    Returns (source, [pairs per stage])."""
+    S = len(pe.stages)
+    if S < 2:
+        raise FormuraCompileError("single-stage programs use the one-pass adjoint")
+    stage_of = {n.omid: s.index for s in pe.stages for n in s.nodes}
+    fields = pe.fields
+    an = pe.an
+    shift3 = [pe.shift if i >= 3 - pe.dim else 0 for i in range(3)]
+    pass1: List[str] = []
+    pair_lists: List[List[tuple]] = []
+    for st in pe.stages:
+        se = _StageEmitter(pe, st)
+        for node in st.nodes:
+            se.node(node)       # the forward at p; its stores are no-ops in the adjoint accessor
+        defs: Dict[tuple, tuple] = {}
+        order: List[tuple] = []
+        for node in st.nodes:
+            for idx, mn in enumerate(node.micro):
+                if mn.key not in defs:
+                    defs[mn.key] = (node, idx)
+                    order.append(mn.key)
+        alg = _Algebra(se, pe)
+        bar: Dict[tuple, List[tuple]] = {}
+        for node in st.nodes:
+            if node.is_store:
+                store = node.micro[-1]
+                f = fields.index(store.inst[1])
+                lam = se.bind(f"a.template ldl<{f}, {shift3[0]}, {shift3[1]}, {shift3[2]}>()")
+                bar.setdefault(node.micro[store.inst[2]].key, []).append(lam)
+            if node.omid in st.mid_out:
+                k = pe.mids.index(node.omid)
+                lam = se.bind(f"a.template ldlm<{k}>()")
+                bar.setdefault(node.micro[-1].key, []).append(lam)
+        pairs: List[tuple] = []
+        pair_val: Dict[tuple, tuple] = {}
+
+        def value(key):
+            return _as_alg(se.var[key])
+
+        for key in reversed(order):
+            if key not in bar:
+                continue
+            node, i = defs[key]
+            micro = node.micro
+            inst = micro[i].inst
+            k = inst[0]
+            total = bar[key][0]
+            for t in bar[key][1:]:
+                total = alg.add(total, t)
+            if k == "loadstatic" or (k == "loadcursor" and stage_of[inst[2]] != st.index):
+                kind = ("s", fields.index(inst[2])) if k == "loadstatic" else ("m", pe.mids.index(inst[2]))
+                pair = kind + (tuple(pe.cursor3(inst[1])),)
+                if pair in pair_val:
+                    pair_val[pair] = alg.add(pair_val[pair], total)
+                else:
+                    pairs.append(pair)
+                    pair_val[pair] = total
+                continue
+            if k in ("imm", "loadindex", "store", "loadcursor"):
+                continue
+            if an.om_uniform(key[1]):
+                continue
+            Y = total
+
+            def opk(j, micro=micro):
+                return micro[j].key
+
+            def push(j, v, micro=micro):
+                mj = micro[j]
+                if mj.inst[0] in ("loadstatic", "loadcursor") or not an.om_uniform(mj.key[1]):
+                    bar.setdefault(mj.key, []).append(v())
+
+            if k == "uniop":
+                op, a = inst[1], inst[2]
+                if op == "+":
+                    push(a, lambda: Y)
+                elif op == "-":
+                    push(a, lambda: alg.neg(Y))
+                else:
+                    fn = op[len("external-call/"):]
+                    x = alg.T(value(opk(a)))
+                    y = alg.T(value(key))
+                    d = {"sqrt": f"M::div(T(0.5), {y})", "exp": y, "log": f"M::div(T(1), {x})",
+                         "sin": f"M::cos({x})", "cos": f"M::neg(M::sin({x}))",
+                         "fabs": f"({x} < T(0) ? T(-1) : T(1))"}.get(fn)
+                    if d is None:
+                        raise FormuraCompileError(f"no derivative for {fn}")
+                    push(a, lambda: alg.mul(Y, se.bind(d)))
+            elif k == "binop":
+                op, a, b = inst[1], inst[2], inst[3]
+                if op in _CMP:
+                    continue
+                if op == "+":
+                    push(a, lambda: Y)
+                    push(b, lambda: Y)
+                elif op == "-":
+                    push(a, lambda: Y)
+                    push(b, lambda: alg.neg(Y))
+                elif op == "*":
+                    push(a, lambda: alg.mul(Y, value(opk(b))))
+                    push(b, lambda: alg.mul(Y, value(opk(a))))
+                elif op == "/":
+                    push(a, lambda: alg.div(Y, value(opk(b))))
+                    if not an.om_uniform(micro[b].key[1]) or micro[b].inst[0] in ("loadstatic", "loadcursor"):
+                        push(b, lambda: alg.neg(alg.div(alg.mul(Y, value(key)), value(opk(b)))))
+                elif op == "**":
+                    A, B = alg.T(value(opk(a))), alg.T(value(opk(b)))
+                    push(a, lambda: alg.mul(Y, se.bind(f"M::mul({B}, M::pow({A}, M::sub({B}, T(1))))")))
+                    if not an.om_uniform(micro[b].key[1]):
+                        push(b, lambda: alg.mul(Y, se.bind(f"M::mul({alg.T(value(key))}, M::log({A}))")))
+                else:
+                    raise FormuraCompileError(f"no derivative for {op}")
+            elif k == "triop":
+                c, a, b = inst[2], inst[3], inst[4]
+                C = se.as_bool(value(opk(c)))
+                push(a, lambda: se.bind(f"({C} ? {alg.T(Y)} : T(0))"))
+                push(b, lambda: se.bind(f"({C} ? T(0) : {alg.T(Y)})"))
+        for j, pair in enumerate(pairs):
+            se.emit(f"a.template stp<{j}>({alg.T(pair_val[pair])});")
+        pair_lists.append(pairs)
+        body = "\n".join(se.lines)
+        pass1.append(f"struct AdjStage{st.index} {{\n"
+                     f"  static constexpr int kPairs = {len(pairs)};\n"
+                     f"  template <class M, class A>\n"
+                     f"  static __device__ __forceinline__ void run(const A& a, const typename M::T* __restrict__ U) {{\n"
+                     f"    using T = typename M::T;\n    (void)U;\n{body}\n  }}\n}};\n")
+    # gathers, in the order the adjoint runs them (last stage first)
+    written = set()
+    gathers: Dict[int, str] = {}
+    for st in reversed(pe.stages):
+        pairs = pair_lists[st.index]
+        targets: Dict[tuple, List[int]] = {}
+        for j, p in enumerate(pairs):
+            targets.setdefault(p[:2], []).append(j)
+        lines = []
+        for tgt in sorted(targets):
+            terms = [f"a.template ldp<{j}, {-pairs[j][2][0]}, {-pairs[j][2][1]}, {-pairs[j][2][2]}>()"
+                     for j in targets[tgt]]
+            expr = terms[0]
+            for t in terms[1:]:
+                expr = f"M::add({expr}, {t})"
+            first = "true" if tgt not in written else "false"
+            written.add(tgt)
+            fn = "accs" if tgt[0] == "s" else "accm"
+            lines.append(f"    a.template {fn}<{tgt[1]}, {first}>({expr});")
+        if st.index == 0:
+            for g in range(len(fields)):
+                if ("s", g) not in written:
+                    lines.append(f"    a.template accs<{g}, true>(T(0));")
+        gathers[st.index] = (f"struct AdjGather{st.index} {{\n"
+                             f"  template <class M, class A>\n"
+                             f"  static __device__ __forceinline__ void run(const A& a, const typename M::T* __restrict__ U) {{\n"
+                             f"    using T = typename M::T;\n    (void)U;\n" + "\n".join(lines) + "\n  }\n};\n")
+    src = "\n".join(pass1[s] + gathers[s] for s in range(S))
+    pairs_list = ", ".join(f"fgb::AdjointStagePair<AdjStage{s}, AdjGather{s}>" for s in range(S))
+    src += f"using StageAdjointList = fgb::AdjointStages<{pairs_list}>;\n"
+    return src, pair_lists

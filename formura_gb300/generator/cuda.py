@@ -525,7 +525,8 @@ class _StageEmitter:
 
 
 class _ProgramEmitter:
-    def __init__(self, mm: MMProgram, name: str, runtime_params: List[str], graph: str = "step"):
+    def __init__(self, mm: MMProgram, name: str, runtime_params: List[str], graph: str = "step",
+                 stage_adjoint: bool = False):
         self.mm = mm
         self.name = name
         self.graph = graph
@@ -545,6 +546,8 @@ class _ProgramEmitter:
         self.table: List[tuple] = []
         self.scaled_cache: Dict[int, dict] = {}
         self.soft_cost = soft_cost_default()
+        self.stage_adjoint = stage_adjoint
+        self.adjoint_pairs: List[List[tuple]] = []
         rng = calc_range(self.mmg)
         s = self.sleeve
         stores = [n for n in self.mmg if n.is_store]
@@ -592,16 +595,23 @@ class _ProgramEmitter:
                 f"    using T = typename M::T;\n"
                 f"    (void)U;\n{body}\n  }}\n}};\n")
         adj_src = None
+        stage_adj = None
         if self.graph == "step" and len(self.stages) == 1 and not self.mids:
             from .adjoint import emit_adjoint
             try:
                 adj_src, _ = emit_adjoint(self.mm, self.name, self)
             except FormuraCompileError:
                 adj_src = None
+        elif self.graph == "step" and self.stage_adjoint:
+            from .adjoint import emit_stage_adjoints
+            stage_adj, self.adjoint_pairs = emit_stage_adjoints(self)
         if adj_src:
             out.append(adj_src)
+        if stage_adj:
+            out.append(stage_adj)
         out.append(f"struct Prog {{\n"
-                   f"  using Adjoint = {'Adjoint' if adj_src else 'void'};\n"
+                   f"  using Adjoint = {'AdjointStep' if adj_src else 'void'};\n"
+                   f"  using StageAdjoint = {'StageAdjointList' if stage_adj else 'void'};\n"
                    f"  static constexpr int kDim = {self.dim};\n"
                    f"  static constexpr int kFields = {len(self.fields)};\n"
                    f"  static constexpr int kMids = {len(self.mids)};\n"
@@ -622,12 +632,27 @@ class _ProgramEmitter:
                              self.mids, list(self.table), self.runtime_params, "\n".join(out) + "\n")
 
 
+def library_option(program: str, key: str, default=None):
+    """A gpu_* option of a program shipped in formura_gb300/programs (the
+    library's kernels were generated with it), or `default`."""
+    from .config import decode_config
+    path = os.path.join(os.path.dirname(os.path.dirname(os.path.abspath(__file__))), "programs", program + ".yaml")
+    if not os.path.exists(path):
+        return default
+    with open(path) as f:
+        return decode_config(f.read()).gpu.get(key, default)
+
+
 def emit_cuda(mm: MMProgram, name: str, runtime_params: Optional[List[str]] = None,
-              graph: str = "step") -> KernelProgram:
+              graph: str = "step", stage_adjoint: Optional[bool] = None) -> KernelProgram:
     """Device code of the step function (or of first_step / filter, which
-    become library programs named <name>__first_step / <name>__filter)."""
+    become library programs named <name>__first_step / <name>__filter).
+    Multi-stage steps get an adjoint when `stage_adjoint` is set; by default
+    when the library's program sets `gpu_adjoint: 1`."""
+    if stage_adjoint is None:
+        stage_adjoint = bool(library_option(name, "gpu_adjoint", 0))
     kp = _ProgramEmitter(mm, name if graph == "step" else f"{name}__{graph}",
-                         runtime_params or [], graph).emit()
+                         runtime_params or [], graph, stage_adjoint and graph == "step").emit()
     kp.graph = graph
     return kp
 
