@@ -370,13 +370,16 @@ struct FusedFill {
         d.nbatch[P] = 0;
       }
     } else if constexpr (Prog::kDim == 3 && Prog::kStages == 1 && Prog::kMids == 0) {
+      // tile widths with tile + 2 * halo a multiple of the warp width, so
+      // that the 32-lane rows of the CTA cover each level without idle lanes
+      constexpr int R = Prog::kReach;
       const FgbFusedVariant v[] = {
-          Tb3dVariant<Prog, P, Stage0, 64, 16, 2>::describe(),
-          Tb3dVariant<Prog, P, Stage0, 64, 16, 4>::describe(),
-          Tb3dVariant<Prog, P, Stage0, 32, 32, 4>::describe(),
-          Tb3dVariant<Prog, P, Stage0, 64, 32, 4>::describe(),
-          Tb3dVariant<Prog, P, Stage0, 128, 16, 4>::describe(),
-          Tb3dVariant<Prog, P, Stage0, 32, 16, 8>::describe(),
+          Tb3dVariant<Prog, P, Stage0, 64 - 4 * R, 16, 2>::describe(),
+          Tb3dVariant<Prog, P, Stage0, 64 - 8 * R, 24, 4>::describe(),
+          Tb3dVariant<Prog, P, Stage0, 64 - 8 * R, 16, 4>::describe(),
+          Tb3dVariant<Prog, P, Stage0, 128 - 8 * R, 16, 4>::describe(),
+          Tb3dVariant<Prog, P, Stage0, 64 - 4 * R, 24, 2>::describe(),
+          Tb3dVariant<Prog, P, Stage0, 64 - 16 * R, 16, 8>::describe(),
       };
       d.nfused[P] = (int)(sizeof v / sizeof v[0]);
       for (int i = 0; i < d.nfused[P]; ++i) d.fused[P][i] = v[i];
