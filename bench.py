@@ -104,6 +104,22 @@ class ClockSampler:
                 "reasons": sorted(reasons), "samples": len(self.samples)}
 
 
+def max_over_ranks(x: float, ws: int, device: str) -> float:
+    """The slowest rank's time: every replica must finish its steps."""
+    if ws <= 1:
+        return x
+    import torch
+    t = torch.tensor([x], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def whole_job_rate(cells_per_rank: int, time_steps: int, ms: float, ws: int) -> float:
+    """GLUP/s of the whole job: ws replicas, each advancing its own grid of
+    cells_per_rank points by time_steps, in ms (the max over ranks)."""
+    return ws * cells_per_rank * time_steps / (ms / 1e3) / 1e9
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -327,13 +343,10 @@ def run_ours(args, spec):
     flush = flush_for(args.precision)
     ms, launches = time_grid(g, spf, args.warmup, args.steps, torch, stream, flush)
     clocks = sampler.stop()
-    if ws > 1:
-        t = torch.tensor([ms], device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        ms = float(t.item())
+    ms = max_over_ranks(ms, ws, "cuda")
     final64 = g.download()
     tsteps = args.steps * spf
-    value = ws * cells * tsteps / (ms / 1e3) / 1e9
+    value = whole_job_rate(cells, tsteps, ms, ws)
 
     # roofline: algorithmic bytes per lattice update (one read and one write
     # of every state field, no credit for temporal reuse) times the updates

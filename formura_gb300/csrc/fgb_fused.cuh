@@ -145,12 +145,12 @@ __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ F
   }
 }
 
-template <class Prog, int P, class Stage, int TX, int TY, int K, int RB = 1>
+template <class Prog, int P, class Stage, int TX, int TY, int K, int RB = 1, int BY_ = 8>
 struct Tb2dVariant {
   using M = typename Precision<P>::M;
   using S = typename Precision<P>::S;
   using T = typename M::T;
-  static constexpr int BX = 32, BY = 8;
+  static constexpr int BX = 32, BY = BY_;
   static constexpr int H = K * Prog::kReach;
   static constexpr size_t kSmem = (size_t)2 * Prog::kFields * (TY + 2 * H) * (TX + 2 * H) * sizeof(T);
 
@@ -162,13 +162,8 @@ struct Tb2dVariant {
       if (e != cudaSuccess) return e;
       configured = true;
     }
-    // enough CTAs to fill the SMs several times over; each chunk re-reads
-    // 2H halo planes, so chunks stay at least 4H planes deep
-    const int gx = (L->n[2] + TX - 1) / TX, gy = (L->n[1] + TY - 1) / TY;
-    const int want = (1216 + gx * gy - 1) / (gx * gy);
-    const int most = L->n[0] / (4 * H) > 1 ? L->n[0] / (4 * H) : 1;
-    const int gz = want < most ? want : most;
-    kern<<<dim3(gx, gy, gz), dim3(BX, BY), kSmem, stream>>>(*L);
+    dim3 grid((L->n[2] + TX - 1) / TX, (L->n[1] + TY - 1) / TY, 1);
+    kern<<<grid, dim3(BX, BY), kSmem, stream>>>(*L);
     return cudaGetLastError();
   }
   static FgbFusedVariant describe() {
@@ -298,22 +293,23 @@ struct Tb2dBatchVariant {
 // pick the ring slot, loads across it read the tile.
 template <class T, int NF, int P, int RY, int RX>
 struct PlaneAccess {
-  const T* level;   // ring of the level below: [P][NF][RY][RX]
-  int z, ly, lx;    // plane (position along the streamed axis), tile cell
+  const T* const* plane;  // the 2R+1 planes of the level below, z - R .. z + R
+  int cell;               // ly * RX + lx
   T* res;
-  __device__ __forceinline__ static int slot(int z) {
-    int r = z % P;
-    return r < 0 ? r + P : r;
-  }
   template <int F, int D0, int D1, int D2>
   __device__ __forceinline__ T ld() const {
-    return level[((slot(z + D0) * NF + F) * RY + ly + D1) * RX + lx + D2];
+    return plane[D0 + P / 2][F * RY * RX + cell + D1 * RX + D2];
   }
   template <int F>
   __device__ __forceinline__ void st(T v) const {
     res[F] = v;
   }
 };
+
+__device__ __forceinline__ int ring_slot(int z, int p) {
+  const int r = z % p;
+  return r < 0 ? r + p : r;
+}
 
 template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY>
 __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ FgbLaunch L) {
@@ -341,7 +337,7 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
   for (int zin = z0 - H; zin < z1 + H; ++zin) {
     {  // level 0: load the plane (periodic in all axes)
       const int gz = small ? pmod(zin, nz) : pwrap(zin, nz);
-      T* dst = rings + PlaneAccess<T, NF, P, RY, RX>::slot(zin) * PL;
+      T* dst = rings + ring_slot(zin, P) * PL;
       for (int ly = threadIdx.y; ly < RY; ly += BY) {
         const int gy = small ? pmod(y0 - H + ly, ny) : pwrap(y0 - H + ly, ny);
         for (int lx = threadIdx.x; lx < RX; lx += BX) {
@@ -359,13 +355,16 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
       const int zt = zin - t * R;
       if (zt < z0 - (K - t) * R) break;   // this level has nothing to compute yet
       const T* below = rings + (size_t)(t - 1) * P * PL;
+      const T* planes[P];
+#pragma unroll
+      for (int j = 0; j < P; ++j) planes[j] = below + ring_slot(zt - R + j, P) * PL;
       const int lo = t * R;
       if (t < K) {
-        T* mine = rings + (size_t)t * P * PL + PlaneAccess<T, NF, P, RY, RX>::slot(zt) * PL;
+        T* mine = rings + (size_t)t * P * PL + ring_slot(zt, P) * PL;
         for (int ly = lo + threadIdx.y; ly < RY - lo; ly += BY) {
           for (int lx = lo + threadIdx.x; lx < RX - lo; lx += BX) {
             T res[NF];
-            PlaneAccess<T, NF, P, RY, RX> a{below, zt, ly, lx, res};
+            PlaneAccess<T, NF, P, RY, RX> a{planes, ly * RX + lx, res};
             Stage::template run<M>(a, U);
 #pragma unroll
             for (int f = 0; f < NF; ++f) mine[(f * RY + ly) * RX + lx] = res[f];
@@ -383,7 +382,7 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
             if (px >= nx) break;
             const int ox = small ? (px + K * Prog::kShift) % nx : pwrap(px + K * Prog::kShift, nx);
             T res[NF];
-            PlaneAccess<T, NF, P, RY, RX> a{below, zt, ty + H, tx + H, res};
+            PlaneAccess<T, NF, P, RY, RX> a{planes, (ty + H) * RX + tx + H, res};
             Stage::template run<M>(a, U);
             const size_t g = ((size_t)oz * ny + oy) * nx + ox;
 #pragma unroll

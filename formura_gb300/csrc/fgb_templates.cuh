@@ -343,15 +343,19 @@ struct FusedFill {
   template <int P>
   static void fill(FgbProgramDesc& d) {
     if constexpr (Prog::kDim == 2 && Prog::kStages == 1 && Prog::kMids == 0) {
+      // (tile x, tile y, steps, rows per thread, thread rows).  The
+      // warp-aligned shapes keep the first step's region (tile + 2(K-1)R)
+      // within one pass of the CTA's rows and within whole 32-lane passes.
+      constexpr int R = Prog::kReach;
       const FgbFusedVariant v[] = {
           Tb2dVariant<Prog, P, Stage0, 64, 32, 2>::describe(),
           Tb2dVariant<Prog, P, Stage0, 64, 32, 4>::describe(),
-          Tb2dVariant<Prog, P, Stage0, 64, 64, 4>::describe(),
-          Tb2dVariant<Prog, P, Stage0, 128, 32, 4>::describe(),
+          Tb2dVariant<Prog, P, Stage0, 64 - 6 * R, 32 - 6 * R, 4, 4>::describe(),
+          Tb2dVariant<Prog, P, Stage0, 64 - 6 * R, 64 - 6 * R, 4, 4, 16>::describe(),
           Tb2dVariant<Prog, P, Stage0, 64, 32, 4, 4>::describe(),
-          Tb2dVariant<Prog, P, Stage0, 64, 64, 4, 4>::describe(),
-          Tb2dVariant<Prog, P, Stage0, 128, 64, 8, 4>::describe(),
-          Tb2dVariant<Prog, P, Stage0, 64, 64, 8, 2>::describe(),
+          Tb2dVariant<Prog, P, Stage0, 64 - 2 * R, 64 - 2 * R, 2, 4, 16>::describe(),
+          Tb2dVariant<Prog, P, Stage0, 64 - 14 * R, 64 - 14 * R, 8, 4, 16>::describe(),
+          Tb2dVariant<Prog, P, Stage0, 128 - 6 * R, 64 - 6 * R, 4, 4, 16>::describe(),
       };
       d.nfused[P] = (int)(sizeof v / sizeof v[0]);
       for (int i = 0; i < d.nfused[P]; ++i) d.fused[P][i] = v[i];
