@@ -333,23 +333,52 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
   const bool small = TY + H >= ny || TX + H >= nx || H >= nz || K * Prog::kShift >= nx ||
                      K * Prog::kShift >= ny || K * Prog::kShift >= nz;
 
-  // input planes run over [z0 - H, z1 + H); level t works on plane zin - t*R
-  for (int zin = z0 - H; zin < z1 + H; ++zin) {
-    {  // level 0: load the plane (periodic in all axes)
-      const int gz = small ? pmod(zin, nz) : pwrap(zin, nz);
-      T* dst = rings + ring_slot(zin, P) * PL;
-      for (int ly = threadIdx.y; ly < RY; ly += BY) {
-        const int gy = small ? pmod(y0 - H + ly, ny) : pwrap(y0 - H + ly, ny);
-        for (int lx = threadIdx.x; lx < RX; lx += BX) {
+  // Input planes run over [z0 - H, z1 + H); level t works on plane
+  // zin - t*R.  The next input plane is fetched into registers while the
+  // levels of the current one are computed, so its HBM latency is hidden.
+  constexpr int NI = (RY + BY - 1) / BY, NJ = (RX + BX - 1) / BX;
+  static_assert(K >= 2, "the level-0 ring is refilled after level 1 has read it");
+  T pre[NI][NJ][NF];
+  auto fetch = [&](int zin) {
+    const int gz = small ? pmod(zin, nz) : pwrap(zin, nz);
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+      const int ly = threadIdx.y + i * BY;
+      const int gy = small ? pmod(y0 - H + ly, ny) : pwrap(y0 - H + ly, ny);
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        const int lx = threadIdx.x + j * BX;
+        if (ly < RY && lx < RX) {
           const int gx = small ? pmod(x0 - H + lx, nx) : pwrap(x0 - H + lx, nx);
           const size_t g = ((size_t)gz * ny + gy) * nx + gx;
 #pragma unroll
           for (int f = 0; f < NF; ++f)
-            dst[(f * RY + ly) * RX + lx] = Storage<S, T>::load(static_cast<const S*>(L.in[f])[g], L.scale[f]);
+            pre[i][j][f] = Storage<S, T>::load(static_cast<const S*>(L.in[f])[g], L.scale[f]);
         }
       }
     }
-    __syncthreads();
+  };
+  auto put = [&](int zin) {
+    T* dst = rings + ring_slot(zin, P) * PL;
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+      const int ly = threadIdx.y + i * BY;
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        const int lx = threadIdx.x + j * BX;
+        if (ly < RY && lx < RX) {
+#pragma unroll
+          for (int f = 0; f < NF; ++f) dst[(f * RY + ly) * RX + lx] = pre[i][j][f];
+        }
+      }
+    }
+  };
+  fetch(z0 - H);
+  put(z0 - H);
+  __syncthreads();
+  for (int zin = z0 - H; zin < z1 + H; ++zin) {
+    const bool more = zin + 1 < z1 + H;
+    if (more) fetch(zin + 1);
 #pragma unroll 1
     for (int t = 1; t <= K; ++t) {
       const int zt = zin - t * R;
@@ -370,6 +399,7 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
             for (int f = 0; f < NF; ++f) mine[(f * RY + ly) * RX + lx] = res[f];
           }
         }
+        __syncthreads();
       } else {
         // final level: the tile's cells of plane zt, straight to HBM
         const int oz = small ? (zt + K * Prog::kShift) % nz : pwrap(zt + K * Prog::kShift, nz);
@@ -391,8 +421,10 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
           }
         }
       }
-      __syncthreads();
     }
+    // level 1 has read the ring slot that plane zin + 1 takes over
+    if (more) put(zin + 1);
+    __syncthreads();
   }
 }
 

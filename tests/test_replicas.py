@@ -31,7 +31,7 @@ def _rank_main(rank, ws, port, out):
 def test_max_over_ranks_and_whole_job_rate_gloo():
     ws = 2
     port = 29500 + os.getpid() % 2000
-    with mp.Manager() as m:
+    with mp.get_context("spawn").Manager() as m:
         out = m.dict()
         mp.start_processes(_rank_main, args=(ws, port, out), nprocs=ws, start_method="spawn", join=True)
         res = dict(out)
