@@ -61,7 +61,48 @@ __device__ __forceinline__ int pwrap(int a, int n) {
   return a >= n ? a - n : a;
 }
 
-template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY, int RB>
+// TMA load of one tile (with halo) per field into shared memory: one
+// elected thread arms an mbarrier with the expected bytes and issues one 2D
+// box copy per field; every thread waits on the barrier with a bounded
+// number of polls.  Returns false (and raises the launch's error flag) if the
+// wait ran out.  The box lies inside the grid: the caller checks that.
+template <class T, int NF, int PLANE>
+__device__ __forceinline__ bool tma_load_tile(const FgbLaunch& L, T* smem, int x, int y) {
+  __shared__ __align__(8) uint64_t bar;
+  const uint32_t b = (uint32_t)__cvta_generic_to_shared(&bar);
+  const bool leader = threadIdx.x == 0 && threadIdx.y == 0;
+  if (leader) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(b) : "memory");
+    asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+  }
+  __syncthreads();
+  if (leader) {
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b),
+                 "r"((uint32_t)(NF * PLANE * sizeof(T)))
+                 : "memory");
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      const char* map = static_cast<const char*>(L.tmap) + f * FGB_TMA_MAP_BYTES;
+      const uint32_t dst = (uint32_t)__cvta_generic_to_shared(smem + f * PLANE);
+      asm volatile(
+          "cp.async.bulk.tensor.2d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3}], [%4];" ::"r"(dst),
+          "l"(map), "r"(x), "r"(y), "r"(b)
+          : "memory");
+    }
+  }
+  uint32_t done = 0;
+  for (int it = 0; it < (1 << 20) && !done; ++it)
+    asm volatile(
+        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+        : "=r"(done)
+        : "r"(b), "r"(0u)
+        : "memory");
+  const bool ok = __syncthreads_and(done != 0);
+  if (!ok && leader && L.err) atomicExch(L.err, 1);
+  return ok;
+}
+
+template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY, int RB, bool TMA>
 __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ FgbLaunch L) {
   using T = typename M::T;
   constexpr int NF = Prog::kFields;
@@ -71,25 +112,40 @@ __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ F
   constexpr int PLANE = RY * RX;
   static_assert(Prog::kShift >= 0, "the per-step roll is non-negative");
   extern __shared__ __align__(16) unsigned char fgb_smem_raw[];
-  T* smem = reinterpret_cast<T*>(fgb_smem_raw);
+  // TMA writes to 128-byte aligned shared memory: the variant allocates 128
+  // spare bytes and the tile starts at the next 128-byte boundary
+  const uint32_t base = (uint32_t)__cvta_generic_to_shared(fgb_smem_raw);
+  T* smem = reinterpret_cast<T*>(fgb_smem_raw + (TMA ? ((128u - (base & 127u)) & 127u) : 0u));
   const int ny = L.n[1], nx = L.n[2];
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const T* __restrict__ U = static_cast<const T*>(L.uniforms);
 
   // load the tile and its halo (periodic); halos shorter than the grid use
-  // the cheap wrap
+  // the cheap wrap.  Tiles whose halo lies inside the grid come by TMA.
   const bool small = TY + H >= ny || TX + H >= nx || K * Prog::kShift >= ny || K * Prog::kShift >= nx;
-  for (int ly = threadIdx.y; ly < RY; ly += BY) {
-    const int gy = small ? pmod(y0 - H + ly, ny) : pwrap(y0 - H + ly, ny);
-    for (int lx = threadIdx.x; lx < RX; lx += BX) {
-      const int gx = small ? pmod(x0 - H + lx, nx) : pwrap(x0 - H + lx, nx);
-      const uint32_t g = (uint32_t)gy * (uint32_t)nx + (uint32_t)gx;
-#pragma unroll
-      for (int f = 0; f < NF; ++f)
-        smem[f * PLANE + ly * RX + lx] = Storage<S, T>::load(static_cast<const S*>(L.in[f])[g], L.scale[f]);
+  bool loaded = false;
+  if constexpr (TMA) {
+    static_assert(RX == FGB_TMA_BOX && RY == FGB_TMA_BOX, "the tensor maps' box is the tile with its halo");
+    static_assert(std::is_same<S, T>::value && (H * sizeof(T)) % 16 == 0 && (TX * sizeof(T)) % 16 == 0,
+                  "box starts on a 16-byte boundary");
+    if (L.tmap != nullptr && x0 >= H && y0 >= H && x0 + TX + H <= nx && y0 + TY + H <= ny) {
+      if (!tma_load_tile<T, NF, PLANE>(L, smem, x0 - H, y0 - H)) return;
+      loaded = true;
     }
   }
-  __syncthreads();
+  if (!loaded) {
+    for (int ly = threadIdx.y; ly < RY; ly += BY) {
+      const int gy = small ? pmod(y0 - H + ly, ny) : pwrap(y0 - H + ly, ny);
+      for (int lx = threadIdx.x; lx < RX; lx += BX) {
+        const int gx = small ? pmod(x0 - H + lx, nx) : pwrap(x0 - H + lx, nx);
+        const uint32_t g = (uint32_t)gy * (uint32_t)nx + (uint32_t)gx;
+#pragma unroll
+        for (int f = 0; f < NF; ++f)
+          smem[f * PLANE + ly * RX + lx] = Storage<S, T>::load(static_cast<const S*>(L.in[f])[g], L.scale[f]);
+      }
+    }
+    __syncthreads();
+  }
 
 #pragma unroll 1
   for (int k = 0; k < K; ++k) {
@@ -145,17 +201,18 @@ __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ F
   }
 }
 
-template <class Prog, int P, class Stage, int TX, int TY, int K, int RB = 1, int BY_ = 8>
+template <class Prog, int P, class Stage, int TX, int TY, int K, int RB = 1, int BY_ = 8, bool TMA = false>
 struct Tb2dVariant {
   using M = typename Precision<P>::M;
   using S = typename Precision<P>::S;
   using T = typename M::T;
   static constexpr int BX = 32, BY = BY_;
   static constexpr int H = K * Prog::kReach;
-  static constexpr size_t kSmem = (size_t)2 * Prog::kFields * (TY + 2 * H) * (TX + 2 * H) * sizeof(T);
+  static constexpr size_t kSmem =
+      (size_t)2 * Prog::kFields * (TY + 2 * H) * (TX + 2 * H) * sizeof(T) + (TMA ? 128 : 0);
 
   static cudaError_t launch(const FgbLaunch* L, cudaStream_t stream) {
-    auto kern = tb2d_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY, RB>;
+    auto kern = tb2d_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY, RB, TMA>;
     static bool configured = false;
     if (!configured) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);

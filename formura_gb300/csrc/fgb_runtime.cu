@@ -2,6 +2,7 @@
 // transfer of formura_data, and the time loop that replaces
 // Formura_Forward's halo assembly + OpenMP loop nests
 // (src/Formura/Generator/Templates.hs:295-346).
+#include <cuda.h>
 #include <cuda_runtime.h>
 #include <cuda_fp16.h>
 #include <stdarg.h>
@@ -119,6 +120,8 @@ struct fgb_grid {
   int lcur = 0;
   void* lam_mids = nullptr;             // multi-stage adjoint: adjoints of the forward arrays
   void* pairs = nullptr;                // and the partial sums of one stage (compute type)
+  void* tmaps = nullptr;                // TMA tensor maps [2 state buffers][nfields], or null
+  int* err = nullptr;                   // device flag of bounded waits that ran out
   std::vector<void*> snaps;             // checkpoints of the forward state
   int grad_steps = -1;                  // steps recorded by fgb_gradient_forward
   int64_t grad_fwd = 0, grad_adj = 0;   // forward steps (incl. recomputation) and adjoint steps
@@ -145,6 +148,61 @@ static void fill_launch(const fgb_grid* g, int cur, FgbLaunch* L) {
   L->uniforms = g->uniforms;
   for (int a = 0; a < 3; ++a) L->n[a] = g->n[a];
   L->fused_steps = 1;
+  L->tmap = g->tmaps ? (const char*)g->tmaps + (size_t)cur * g->prog->nfields * FGB_TMA_MAP_BYTES : nullptr;
+  L->err = g->err;
+}
+
+// TMA tensor maps of the two state buffers (2D, FP64/FP32 storage, rows of a
+// multiple of 16 bytes): boxes of FGB_TMA_BOX^2 elements for the tile kernels.
+// Without them (other grids, or no driver entry point) the kernels load
+// their tiles with ordinary loads.
+static void make_tensor_maps(fgb_grid* g) {
+  const FgbProgramDesc* d = g->prog;
+  const size_t es = storage_size(g->precision);
+  if (d->dim != 2 || g->precision > FGB_F32 || (g->n[2] * es) % 16 != 0 || g->n[2] < FGB_TMA_BOX ||
+      g->n[1] < FGB_TMA_BOX)
+    return;
+  static_assert(sizeof(CUtensorMap) == FGB_TMA_MAP_BYTES, "tensor map size");
+  void* fn = nullptr;
+  cudaDriverEntryPointQueryResult q;
+  if (cudaGetDriverEntryPointByVersion("cuTensorMapEncodeTiled", &fn, 12000, cudaEnableDefault, &q) != cudaSuccess ||
+      q != cudaDriverEntryPointSuccess || !fn)
+    return;
+  auto encode = reinterpret_cast<CUresult (*)(CUtensorMap*, CUtensorMapDataType, cuuint32_t, void*, const cuuint64_t*,
+                                              const cuuint64_t*, const cuuint32_t*, const cuuint32_t*,
+                                              CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
+                                              CUtensorMapFloatOOBfill)>(fn);
+  std::vector<CUtensorMap> maps(2 * d->nfields);
+  const cuuint64_t dims[2] = {(cuuint64_t)g->n[2], (cuuint64_t)g->n[1]};
+  const cuuint64_t strides[1] = {(cuuint64_t)g->n[2] * es};
+  const cuuint32_t box[2] = {FGB_TMA_BOX, FGB_TMA_BOX};
+  const cuuint32_t unit[2] = {1, 1};
+  const CUtensorMapDataType type = es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
+  for (int b = 0; b < 2; ++b)
+    for (int f = 0; f < d->nfields; ++f) {
+      void* base = (char*)g->state[b] + f * g->cells * es;
+      if (encode(&maps[b * d->nfields + f], type, 2, base, dims, strides, box, unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
+                 CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
+                 CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
+        return;
+    }
+  void* dev = nullptr;
+  if (cudaMalloc(&dev, maps.size() * sizeof(CUtensorMap)) != cudaSuccess) return;
+  if (cudaMemcpy(dev, maps.data(), maps.size() * sizeof(CUtensorMap), cudaMemcpyHostToDevice) != cudaSuccess) {
+    cudaFree(dev);
+    return;
+  }
+  g->tmaps = dev;
+}
+
+// a kernel's bounded wait ran out: report it once and clear the flag
+static int check_device_flag(fgb_grid* g) {
+  if (!g->err) return FGB_OK;
+  int v = 0;
+  FGB_CUDA(cudaMemcpy(&v, g->err, sizeof v, cudaMemcpyDeviceToHost), "device flag");
+  if (v == 0) return FGB_OK;
+  cudaMemset(g->err, 0, sizeof(int));
+  return fail(FGB_E_CUDA, "a tile kernel's wait for its TMA load ran out (flag %d)", v);
 }
 
 static int run_steps(fgb_grid* g, int nsteps) {
@@ -250,12 +308,15 @@ int fgb_open(const char* program, const int* shape, int ndim, int precision, con
     }
   }
   if (e == cudaSuccess) e = cudaMemsetAsync(g->state[0], 0, cells * d->nfields * es, g->stream);
+  if (e == cudaSuccess) e = cudaMalloc((void**)&g->err, sizeof(int));
+  if (e == cudaSuccess) e = cudaMemsetAsync(g->err, 0, sizeof(int), g->stream);
   if (e == cudaSuccess) e = cudaStreamSynchronize(g->stream);
   if (e != cudaSuccess) {
     int rc = cuda_fail(e, "fgb_open");
     fgb_close(g);
     return rc;
   }
+  make_tensor_maps(g);
   *out = g;
   return FGB_OK;
 }
@@ -273,6 +334,8 @@ int fgb_close(fgb_grid* g) {
   cudaFree(g->lam[1]);
   cudaFree(g->lam_mids);
   cudaFree(g->pairs);
+  cudaFree(g->tmaps);
+  cudaFree(g->err);
   for (auto& sb : g->sub) {
     cudaFree(sb.uniforms);
     cudaFree(sb.mids);
@@ -337,7 +400,7 @@ int fgb_download(fgb_grid* g, double* host) {
     FGB_CUDA(cudaMemcpyAsync(host, g->staging, n * 8, cudaMemcpyDeviceToHost, g->stream), "download");
   }
   FGB_CUDA(cudaStreamSynchronize(g->stream), "download");
-  return FGB_OK;
+  return check_device_flag(g);
 }
 
 int fgb_forward(fgb_grid* g, int nsteps) {
@@ -804,7 +867,7 @@ int fgb_totals(fgb_grid* g, double* sums, int nfields) {
 int fgb_synchronize(fgb_grid* g) {
   if (!g) return fail(FGB_E_ARG, "null grid");
   FGB_CUDA(cudaStreamSynchronize(g->stream), "synchronize");
-  return FGB_OK;
+  return check_device_flag(g);
 }
 
 void* fgb_stream(fgb_grid* g) { return g ? (void*)g->stream : nullptr; }

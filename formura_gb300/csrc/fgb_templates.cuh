@@ -355,7 +355,8 @@ struct FusedFill {
           Tb2dVariant<Prog, P, Stage0, 64, 32, 4, 4>::describe(),
           Tb2dVariant<Prog, P, Stage0, 64 - 2 * R, 64 - 2 * R, 2, 4, 16>::describe(),
           Tb2dVariant<Prog, P, Stage0, 64 - 14 * R, 64 - 14 * R, 8, 4, 16>::describe(),
-          Tb2dVariant<Prog, P, Stage0, 128 - 6 * R, 64 - 6 * R, 4, 4, 16>::describe(),
+          // tiles whose halo is inside the grid arrive by TMA (64 x 64 boxes)
+          Tb2dVariant<Prog, P, Stage0, 64 - 8 * R, 64 - 8 * R, 4, 4, 16, R == 1 && P <= 2>::describe(),
       };
       d.nfused[P] = (int)(sizeof v / sizeof v[0]);
       for (int i = 0; i < d.nfused[P]; ++i) d.fused[P][i] = v[i];
