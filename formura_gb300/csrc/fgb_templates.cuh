@@ -304,11 +304,11 @@ __global__ void __launch_bounds__(kBlockX) adjoint_kernel(const __grid_constant_
   }
 }
 
-// rows per thread: several for the memory-bound FP32/FP16 forms of
-// single-kernel steps, one for FP64 (bound by the FP64 pipe) and for the
-// register-heavy stages of multi-stage programs
+// rows per thread: several for the memory-bound FP32/FP16 forms (four for
+// single-kernel steps, two for the larger stages of multi-stage programs),
+// one for FP64, which is bound by the FP64 pipe
 template <int P, bool Light>
-constexpr int rows_per_thread() { return (P >= 2 && Light) ? 4 : 1; }
+constexpr int rows_per_thread() { return P >= 2 ? (Light ? 4 : 2) : 1; }
 
 template <int P, class Adj>
 cudaError_t launch_adjoint(const FgbLaunch* L, cudaStream_t stream) {
