@@ -260,7 +260,7 @@ def emit_adjoint(mm: MMProgram, name: str, pe: _ProgramEmitter = None):
     body = "\n".join("    " + l.strip() for l in lines) + "\n" + "\n".join(out)
     return (f"struct AdjointStep {{\n"
             f"  template <class M, class A>\n"
-            f"  static __device__ __forceinline__ void run(const A& a, const typename M::T* __restrict__ U) {{\n"
+            f"  static __device__ __forceinline__ void run(const A& a, const typename M::U* __restrict__ U) {{\n"
             f"    using T = typename M::T;\n    (void)U;\n{body}\n  }}\n}};\n"), pe
 
 
@@ -418,7 +418,7 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
         pass1.append(f"struct AdjStage{st.index} {{\n"
                      f"  static constexpr int kPairs = {len(pairs)};\n"
                      f"  template <class M, class A>\n"
-                     f"  static __device__ __forceinline__ void run(const A& a, const typename M::T* __restrict__ U) {{\n"
+                     f"  static __device__ __forceinline__ void run(const A& a, const typename M::U* __restrict__ U) {{\n"
                      f"    using T = typename M::T;\n    (void)U;\n{body}\n  }}\n}};\n")
     # gathers, in the order the adjoint runs them (last stage first)
     written = set()
@@ -445,7 +445,7 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
                     lines.append(f"    a.template accs<{g}, true>(T(0));")
         gathers[st.index] = (f"struct AdjGather{st.index} {{\n"
                              f"  template <class M, class A>\n"
-                             f"  static __device__ __forceinline__ void run(const A& a, const typename M::T* __restrict__ U) {{\n"
+                             f"  static __device__ __forceinline__ void run(const A& a, const typename M::U* __restrict__ U) {{\n"
                              f"    using T = typename M::T;\n    (void)U;\n" + "\n".join(lines) + "\n  }\n};\n")
     src = "\n".join(pass1[s] + gathers[s] for s in range(S))
     pairs_list = ", ".join(f"fgb::AdjointStagePair<AdjStage{s}, AdjGather{s}>" for s in range(S))

@@ -35,6 +35,7 @@ namespace hostshim {
 
 struct Exact {
   using T = double;
+  using U = double;
   static T add(T a, T b) { return a + b; }
   static T sub(T a, T b) { return a - b; }
   static T mul(T a, T b) { return a * b; }
