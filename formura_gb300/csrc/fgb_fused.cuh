@@ -32,31 +32,6 @@ struct TileAccess {
 
 // Two horizontally adjacent points (lx even) for the packed FP32 form: an
 // even x offset is one aligned 8-byte load, an odd one two 4-byte loads.
-// bytes kept free before and after a packed tile (a multiple of 128, so a
-// TMA destination stays aligned)
-constexpr unsigned kPairMargin = 256;
-
-template <int NF, int RY, int RX>
-struct PairTileAccess {
-  const float* cur;
-  f2* res;
-  int ly, lx;
-  template <int F, int D0, int D1, int D2>
-  __device__ __forceinline__ f2 ld() const {
-    static_assert(D0 == 0, "2D tile");
-    const float* p = cur + (F * RY + ly + D1) * RX + lx + D2;
-    if constexpr ((D2 & 1) == 0) {
-      return *reinterpret_cast<const float2*>(p);
-    } else {
-      return make_float2(p[0], p[1]);
-    }
-  }
-  template <int F>
-  __device__ __forceinline__ void st(f2 v) const {
-    res[F] = v;
-  }
-};
-
 // Same tile, but stores go to registers: a thread computes several rows of
 // one column before writing any of them, so loads shared between the rows
 // (the vertical neighbours) are read from shared memory once.
@@ -129,8 +104,7 @@ __device__ __forceinline__ bool tma_load_tile(const FgbLaunch& L, T* smem, int x
   return ok;
 }
 
-template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY, int RB, bool TMA,
-          bool PK>
+template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY, int RB, bool TMA>
 __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ FgbLaunch L) {
   using T = typename M::T;
   constexpr int NF = Prog::kFields;
@@ -142,11 +116,8 @@ __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ F
   extern __shared__ __align__(16) unsigned char fgb_smem_raw[];
   // TMA writes to 128-byte aligned shared memory: the variant allocates 128
   // spare bytes and the tile starts at the next 128-byte boundary
-  // The packed form reads one point past either end of the tile: it keeps a
-  // margin of kPairMargin bytes on both sides.
   const uint32_t base = (uint32_t)__cvta_generic_to_shared(fgb_smem_raw);
-  T* smem = reinterpret_cast<T*>(fgb_smem_raw + (TMA ? ((128u - (base & 127u)) & 127u) : 0u) +
-                                 (PK ? kPairMargin : 0u));
+  T* smem = reinterpret_cast<T*>(fgb_smem_raw + (TMA ? ((128u - (base & 127u)) & 127u) : 0u));
   const int ny = L.n[1], nx = L.n[2];
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   const T* __restrict__ U = static_cast<const T*>(L.uniforms);
@@ -183,32 +154,7 @@ __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ F
     const T* cur = smem + (k & 1) * NF * PLANE;
     T* nxt = smem + ((k + 1) & 1) * NF * PLANE;
     const int lo = (k + 1) * R;
-    if constexpr (PK) {
-      // pairs of points from an even column: when lo is odd the first pair
-      // also computes the point just outside the region (not used later),
-      // and likewise at the right end
-      static_assert(RB > 1 && RX % 2 == 0 && std::is_same<T, float>::value, "packed FP32 tiles");
-      const float* __restrict__ Uf = static_cast<const float*>(L.uniforms);
-      const int last = RY - lo - 1;
-      for (int ly0 = lo + threadIdx.y * RB; ly0 <= last; ly0 += BY * RB) {
-        for (int lx = (lo & ~1) + 2 * threadIdx.x; lx < RX - lo; lx += 2 * BX) {
-          f2 res[RB][NF];
-#pragma unroll
-          for (int r = 0; r < RB; ++r) {
-            PairTileAccess<NF, RY, RX> a{cur, res[r], min(ly0 + r, last), lx};
-            Stage::template run<F32x2>(a, Uf);
-          }
-#pragma unroll
-          for (int r = 0; r < RB; ++r) {
-            if (ly0 + r <= last) {
-#pragma unroll
-              for (int f = 0; f < NF; ++f)
-                *reinterpret_cast<float2*>(nxt + (f * RY + ly0 + r) * RX + lx) = res[r][f].v;
-            }
-          }
-        }
-      }
-    } else if constexpr (RB == 1) {
+    if constexpr (RB == 1) {
       for (int ly = lo + threadIdx.y; ly < RY - lo; ly += BY) {
         for (int lx = lo + threadIdx.x; lx < RX - lo; lx += BX) {
           TileAccess<T, NF, RY, RX> a{cur, nxt, ly, lx};
@@ -257,19 +203,18 @@ __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ F
   }
 }
 
-template <class Prog, int P, class Stage, int TX, int TY, int K, int RB = 1, int BY_ = 8, bool TMA = false,
-          bool PK = false>
+template <class Prog, int P, class Stage, int TX, int TY, int K, int RB = 1, int BY_ = 8, bool TMA = false>
 struct Tb2dVariant {
   using M = typename Precision<P>::M;
   using S = typename Precision<P>::S;
   using T = typename M::T;
   static constexpr int BX = 32, BY = BY_;
   static constexpr int H = K * Prog::kReach;
-  static constexpr size_t kSmem = (size_t)2 * Prog::kFields * (TY + 2 * H) * (TX + 2 * H) * sizeof(T) +
-                                  (TMA ? 128 : 0) + (PK ? 2 * kPairMargin : 0);
+  static constexpr size_t kSmem =
+      (size_t)2 * Prog::kFields * (TY + 2 * H) * (TX + 2 * H) * sizeof(T) + (TMA ? 128 : 0);
 
   static cudaError_t launch(const FgbLaunch* L, cudaStream_t stream) {
-    auto kern = tb2d_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY, RB, TMA, PK>;
+    auto kern = tb2d_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY, RB, TMA>;
     static bool configured = false;
     if (!configured) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);

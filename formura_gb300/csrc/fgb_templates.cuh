@@ -119,71 +119,33 @@ struct F64Fast {
   static __device__ __forceinline__ T pow(T a, T b) { return ::pow(a, b); }
 };
 
-// FP32 arithmetic (used with float or half storage): one rounding per SSA
-// operation, never contracted, so that the packed form below gives the same
-// bits.
+// FP32 arithmetic (used with float or half storage).  The compiler may
+// contract a product and a sum into one FFMA here: FP32 results are checked
+// by their distance to the FP64 form, and every FP32 kernel evaluates the
+// same stage code, so the one-step and the tile kernels still agree bit for
+// bit.
 struct F32 {
   using T = float;
   using U = float;
-  static __device__ __forceinline__ T add(T a, T b) { return __fadd_rn(a, b); }
-  static __device__ __forceinline__ T sub(T a, T b) { return __fsub_rn(a, b); }
-  static __device__ __forceinline__ T mul(T a, T b) { return __fmul_rn(a, b); }
-  static __device__ __forceinline__ T div(T a, T b) { return __fdiv_rn(a, b); }
-  static __device__ __forceinline__ T fma(T a, T b, T c) { return __fmaf_rn(a, b, c); }
-  static __device__ __forceinline__ T divu(T x, T, T rc) { return __fmul_rn(x, rc); }
-  static __device__ __forceinline__ T sadd(T a, T b) { return add(a, b); }
-  static __device__ __forceinline__ T ssub(T a, T b) { return sub(a, b); }
-  static __device__ __forceinline__ T smul(T a, T b) { return mul(a, b); }
-  static __device__ __forceinline__ T sfma(T a, T b, T c) { return fma(a, b, c); }
-  static __device__ __forceinline__ T sdivu(T x, T c, T rc) { return divu(x, c, rc); }
+  static __device__ __forceinline__ T add(T a, T b) { return a + b; }
+  static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
+  static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
+  static __device__ __forceinline__ T div(T a, T b) { return a / b; }
+  static __device__ __forceinline__ T fma(T a, T b, T c) { return fmaf(a, b, c); }
+  static __device__ __forceinline__ T divu(T x, T, T rc) { return x * rc; }
+  static __device__ __forceinline__ T sadd(T a, T b) { return a + b; }
+  static __device__ __forceinline__ T ssub(T a, T b) { return a - b; }
+  static __device__ __forceinline__ T smul(T a, T b) { return a * b; }
+  static __device__ __forceinline__ T sfma(T a, T b, T c) { return fmaf(a, b, c); }
+  static __device__ __forceinline__ T sdivu(T x, T, T rc) { return x * rc; }
   static __device__ __forceinline__ T neg(T a) { return -a; }
-  static __device__ __forceinline__ T sqrt(T a) { return __fsqrt_rn(a); }
+  static __device__ __forceinline__ T sqrt(T a) { return sqrtf(a); }
   static __device__ __forceinline__ T fabs(T a) { return fabsf(a); }
   static __device__ __forceinline__ T exp(T a) { return expf(a); }
   static __device__ __forceinline__ T log(T a) { return logf(a); }
   static __device__ __forceinline__ T sin(T a) { return sinf(a); }
   static __device__ __forceinline__ T cos(T a) { return cosf(a); }
   static __device__ __forceinline__ T pow(T a, T b) { return powf(a, b); }
-};
-
-// Two FP32 lattice points at once on the packed FP32 instructions of this
-// part (FADD2 / FMUL2 / FFMA2): each lane of a pair is rounded exactly like
-// F32, so a kernel that evaluates two neighbouring points per thread gives
-// the same bits with half the arithmetic instructions.  Literals and
-// uniform-table entries broadcast to both lanes.  Programs whose stages
-// compare or select (limiters, Riemann solvers) keep the scalar form.
-struct f2 {
-  float2 v;
-  __device__ __forceinline__ f2() {}
-  __device__ __forceinline__ f2(float2 a) : v(a) {}
-  __device__ __forceinline__ f2(float c) : v(make_float2(c, c)) {}
-  __device__ __forceinline__ f2(double c) : v(make_float2((float)c, (float)c)) {}
-  __device__ __forceinline__ f2(int c) : v(make_float2((float)c, (float)c)) {}
-};
-struct F32x2 {
-  using T = f2;
-  using U = float;
-  static __device__ __forceinline__ T add(T a, T b) { return __fadd2_rn(a.v, b.v); }
-  static __device__ __forceinline__ T sub(T a, T b) { return __fadd2_rn(a.v, make_float2(-b.v.x, -b.v.y)); }
-  static __device__ __forceinline__ T mul(T a, T b) { return __fmul2_rn(a.v, b.v); }
-  static __device__ __forceinline__ T div(T a, T b) {
-    return make_float2(__fdiv_rn(a.v.x, b.v.x), __fdiv_rn(a.v.y, b.v.y));
-  }
-  static __device__ __forceinline__ T fma(T a, T b, T c) { return __ffma2_rn(a.v, b.v, c.v); }
-  static __device__ __forceinline__ T divu(T x, T, T rc) { return mul(x, rc); }
-  static __device__ __forceinline__ T sadd(T a, T b) { return add(a, b); }
-  static __device__ __forceinline__ T ssub(T a, T b) { return sub(a, b); }
-  static __device__ __forceinline__ T smul(T a, T b) { return mul(a, b); }
-  static __device__ __forceinline__ T sfma(T a, T b, T c) { return fma(a, b, c); }
-  static __device__ __forceinline__ T sdivu(T x, T c, T rc) { return divu(x, c, rc); }
-  static __device__ __forceinline__ T neg(T a) { return make_float2(-a.v.x, -a.v.y); }
-  static __device__ __forceinline__ T sqrt(T a) { return make_float2(__fsqrt_rn(a.v.x), __fsqrt_rn(a.v.y)); }
-  static __device__ __forceinline__ T fabs(T a) { return make_float2(fabsf(a.v.x), fabsf(a.v.y)); }
-  static __device__ __forceinline__ T exp(T a) { return make_float2(expf(a.v.x), expf(a.v.y)); }
-  static __device__ __forceinline__ T log(T a) { return make_float2(logf(a.v.x), logf(a.v.y)); }
-  static __device__ __forceinline__ T sin(T a) { return make_float2(sinf(a.v.x), sinf(a.v.y)); }
-  static __device__ __forceinline__ T cos(T a) { return make_float2(cosf(a.v.x), cosf(a.v.y)); }
-  static __device__ __forceinline__ T pow(T a, T b) { return make_float2(powf(a.v.x, b.v.x), powf(a.v.y, b.v.y)); }
 };
 
 // ---------------------------------------------------------------------------
@@ -392,7 +354,6 @@ struct FusedFill {
       // warp-aligned shapes keep the first step's region (tile + 2(K-1)R)
       // within one pass of the CTA's rows and within whole 32-lane passes.
       constexpr int R = Prog::kReach;
-      constexpr bool kPack = P >= 2 && Stage0::kPackable;
       const FgbFusedVariant v[] = {
           Tb2dVariant<Prog, P, Stage0, 64, 32, 2>::describe(),
           Tb2dVariant<Prog, P, Stage0, 64, 32, 4>::describe(),
@@ -400,11 +361,9 @@ struct FusedFill {
           Tb2dVariant<Prog, P, Stage0, 64 - 6 * R, 64 - 6 * R, 4, 4, 16>::describe(),
           Tb2dVariant<Prog, P, Stage0, 64, 32, 4, 4>::describe(),
           Tb2dVariant<Prog, P, Stage0, 64 - 2 * R, 64 - 2 * R, 2, 4, 16>::describe(),
-          // two points per thread on the packed FP32 instructions, where the
-          // stage neither compares nor selects (FP32/FP16 storage)
-          Tb2dVariant<Prog, P, Stage0, 64 - 8 * R, 64 - 8 * R, 4, 4, 16, false, kPack>::describe(),
+          Tb2dVariant<Prog, P, Stage0, 64 - 14 * R, 64 - 14 * R, 8, 4, 16>::describe(),
           // tiles whose halo is inside the grid arrive by TMA (64 x 64 boxes)
-          Tb2dVariant<Prog, P, Stage0, 64 - 8 * R, 64 - 8 * R, 4, 4, 16, R == 1 && P <= 2, kPack>::describe(),
+          Tb2dVariant<Prog, P, Stage0, 64 - 8 * R, 64 - 8 * R, 4, 4, 16, R == 1 && P <= 2>::describe(),
       };
       d.nfused[P] = (int)(sizeof v / sizeof v[0]);
       for (int i = 0; i < d.nfused[P]; ++i) d.fused[P][i] = v[i];

@@ -586,12 +586,10 @@ class _ProgramEmitter:
             for node in st.nodes:
                 se.node(node)
             body = "\n".join(se.lines)
-            # no comparison or selection: the stage can run on pairs of points
-            packable = " bool " not in body and "?" not in body
             stage_texts.append(
                 f"struct Stage{st.index} {{\n"
                 f"  static constexpr bool kWritesState = {'true' if st.writes_state else 'false'};\n"
-                f"  static constexpr bool kPackable = {'true' if packable else 'false'};\n"
+
                 f"  static constexpr int kMidOut = {len(st.mid_out)};\n"
                 f"  template <class M, class A>\n"
                 f"  static __device__ __forceinline__ void run(const A& a, const typename M::U* __restrict__ U) {{\n"
