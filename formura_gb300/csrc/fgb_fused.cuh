@@ -104,6 +104,50 @@ __device__ __forceinline__ bool tma_load_tile(const FgbLaunch& L, T* smem, int x
   return ok;
 }
 
+// K steps of a tile held in shared memory (two buffers of NF planes of
+// RY x RX points).  Step k computes the region that is still exact after k+1
+// steps, (k+1)R points in from the edge.  With RB > 1 a thread computes RB
+// rows of a column into registers before storing any of them, so the
+// vertical neighbours shared by those rows are read once.
+template <class M, class Stage, class T, int NF, int R, int RY, int RX, int K, int BX, int BY, int RB>
+__device__ __forceinline__ void tile_steps(T* smem, const typename M::U* __restrict__ U) {
+  constexpr int PLANE = RY * RX;
+#pragma unroll 1
+  for (int k = 0; k < K; ++k) {
+    const T* cur = smem + (k & 1) * NF * PLANE;
+    T* nxt = smem + ((k + 1) & 1) * NF * PLANE;
+    const int lo = (k + 1) * R;
+    if constexpr (RB == 1) {
+      for (int ly = lo + threadIdx.y; ly < RY - lo; ly += BY) {
+        for (int lx = lo + threadIdx.x; lx < RX - lo; lx += BX) {
+          TileAccess<T, NF, RY, RX> a{cur, nxt, ly, lx};
+          Stage::template run<M>(a, U);
+        }
+      }
+    } else {
+      const int last = RY - lo - 1;   // rows past the region are clamped (computed, not stored)
+      for (int ly0 = lo + threadIdx.y * RB; ly0 <= last; ly0 += BY * RB) {
+        for (int lx = lo + threadIdx.x; lx < RX - lo; lx += BX) {
+          T res[RB][NF];
+#pragma unroll
+          for (int r = 0; r < RB; ++r) {
+            RegTileAccess<T, NF, RY, RX> a{cur, res[r], min(ly0 + r, last), lx};
+            Stage::template run<M>(a, U);
+          }
+#pragma unroll
+          for (int r = 0; r < RB; ++r) {
+            if (ly0 + r <= last) {
+#pragma unroll
+              for (int f = 0; f < NF; ++f) nxt[(f * RY + ly0 + r) * RX + lx] = res[r][f];
+            }
+          }
+        }
+      }
+    }
+    __syncthreads();
+  }
+}
+
 template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY, int RB, bool TMA>
 __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ FgbLaunch L) {
   using T = typename M::T;
@@ -149,40 +193,7 @@ __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ F
     __syncthreads();
   }
 
-#pragma unroll 1
-  for (int k = 0; k < K; ++k) {
-    const T* cur = smem + (k & 1) * NF * PLANE;
-    T* nxt = smem + ((k + 1) & 1) * NF * PLANE;
-    const int lo = (k + 1) * R;
-    if constexpr (RB == 1) {
-      for (int ly = lo + threadIdx.y; ly < RY - lo; ly += BY) {
-        for (int lx = lo + threadIdx.x; lx < RX - lo; lx += BX) {
-          TileAccess<T, NF, RY, RX> a{cur, nxt, ly, lx};
-          Stage::template run<M>(a, U);
-        }
-      }
-    } else {
-      const int last = RY - lo - 1;   // rows past the region are clamped (computed, not stored)
-      for (int ly0 = lo + threadIdx.y * RB; ly0 <= last; ly0 += BY * RB) {
-        for (int lx = lo + threadIdx.x; lx < RX - lo; lx += BX) {
-          T res[RB][NF];
-#pragma unroll
-          for (int r = 0; r < RB; ++r) {
-            RegTileAccess<T, NF, RY, RX> a{cur, res[r], min(ly0 + r, last), lx};
-            Stage::template run<M>(a, U);
-          }
-#pragma unroll
-          for (int r = 0; r < RB; ++r) {
-            if (ly0 + r <= last) {
-#pragma unroll
-              for (int f = 0; f < NF; ++f) nxt[(f * RY + ly0 + r) * RX + lx] = res[r][f];
-            }
-          }
-        }
-      }
-    }
-    __syncthreads();
-  }
+  tile_steps<M, Stage, T, NF, R, RY, RX, K, BX, BY, RB>(smem, U);
 
   // store the tile, rolled by K steps' worth of shift
   const T* fin = smem + (K & 1) * NF * PLANE;
@@ -239,7 +250,7 @@ struct Tb2dVariant {
 // Batched ensemble: persistent CTAs walk a queue of tiles drawn from every
 // grid of the batch; each tile advances K steps in shared memory exactly like
 // tb2d_kernel, with that grid's extent, periodic wrap and uniform table.
-template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY>
+template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY, int RB>
 __global__ void __launch_bounds__(BX * BY) tb2d_batch_kernel(const __grid_constant__ FgbBatchLaunch B) {
   using T = typename M::T;
   constexpr int NF = Prog::kFields;
@@ -270,19 +281,7 @@ __global__ void __launch_bounds__(BX * BY) tb2d_batch_kernel(const __grid_consta
       }
     }
     __syncthreads();
-#pragma unroll 1
-    for (int k = 0; k < K; ++k) {
-      const T* cur = smem + (k & 1) * NF * PLANE;
-      T* nxt = smem + ((k + 1) & 1) * NF * PLANE;
-      const int lo = (k + 1) * R;
-      for (int ly = lo + threadIdx.y; ly < RY - lo; ly += BY) {
-        for (int lx = lo + threadIdx.x; lx < RX - lo; lx += BX) {
-          TileAccess<T, NF, RY, RX> a{cur, nxt, ly, lx};
-          Stage::template run<M>(a, U);
-        }
-      }
-      __syncthreads();
-    }
+    tile_steps<M, Stage, T, NF, R, RY, RX, K, BX, BY, RB>(smem, U);
     const T* fin = smem + (K & 1) * NF * PLANE;
     for (int ty = threadIdx.y; ty < TY; ty += BY) {
       const int py = y0 + ty;
@@ -302,32 +301,32 @@ __global__ void __launch_bounds__(BX * BY) tb2d_batch_kernel(const __grid_consta
   }
 }
 
-template <class Prog, int P, class Stage, int TX, int TY, int K>
+template <class Prog, int P, class Stage, int TX, int TY, int K, int RB = 1, int BY_ = 8>
 struct Tb2dBatchVariant {
   using M = typename Precision<P>::M;
   using S = typename Precision<P>::S;
   using T = typename M::T;
-  static constexpr int BX = 32, BY = 8;
+  static constexpr int BX = 32, BY = BY_;
   static constexpr int H = K * Prog::kReach;
   static constexpr size_t kSmem = (size_t)2 * Prog::kFields * (TY + 2 * H) * (TX + 2 * H) * sizeof(T);
 
   static cudaError_t configure() {
     static cudaError_t state = cudaErrorNotReady;
     if (state == cudaErrorNotReady)
-      state = cudaFuncSetAttribute(tb2d_batch_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY>,
+      state = cudaFuncSetAttribute(tb2d_batch_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY, RB>,
                                    cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);
     return state;
   }
   static cudaError_t launch(const FgbBatchLaunch* B, cudaStream_t stream, int blocks) {
     cudaError_t e = configure();
     if (e != cudaSuccess) return e;
-    tb2d_batch_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY><<<blocks, dim3(BX, BY), kSmem, stream>>>(*B);
+    tb2d_batch_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY, RB><<<blocks, dim3(BX, BY), kSmem, stream>>>(*B);
     return cudaGetLastError();
   }
   static int blocks_per_sm() {
     if (configure() != cudaSuccess) return 0;
     int n = 0;
-    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, tb2d_batch_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY>,
+    if (cudaOccupancyMaxActiveBlocksPerMultiprocessor(&n, tb2d_batch_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY, RB>,
                                                       BX * BY, kSmem) != cudaSuccess)
       return 0;
     return n;

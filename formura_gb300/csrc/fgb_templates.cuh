@@ -370,11 +370,11 @@ struct FusedFill {
       if constexpr (P == 0 || P == 2) {
         const FgbBatchVariant b[] = {
             Tb2dBatchVariant<Prog, P, Stage0, 64, 32, 1>::describe(),
-            Tb2dBatchVariant<Prog, P, Stage0, 64, 32, 2>::describe(),
             Tb2dBatchVariant<Prog, P, Stage0, 64, 32, 4>::describe(),
-            Tb2dBatchVariant<Prog, P, Stage0, 64, 32, 8>::describe(),
-            Tb2dBatchVariant<Prog, P, Stage0, 32, 32, 4>::describe(),
-            Tb2dBatchVariant<Prog, P, Stage0, 128, 32, 4>::describe(),
+            Tb2dBatchVariant<Prog, P, Stage0, 64 - 2 * R, 32 - 2 * R, 2, 4>::describe(),
+            Tb2dBatchVariant<Prog, P, Stage0, 64 - 6 * R, 32 - 6 * R, 4, 4>::describe(),
+            Tb2dBatchVariant<Prog, P, Stage0, 64 - 6 * R, 64 - 6 * R, 4, 4, 16>::describe(),
+            Tb2dBatchVariant<Prog, P, Stage0, 64 - 14 * R, 64 - 14 * R, 8, 4, 16>::describe(),
         };
         d.nbatch[P] = (int)(sizeof b / sizeof b[0]);
         for (int i = 0; i < d.nbatch[P]; ++i) d.batch[P][i] = b[i];
