@@ -130,7 +130,9 @@ struct F32 {
   static __device__ __forceinline__ T add(T a, T b) { return a + b; }
   static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
-  static __device__ __forceinline__ T div(T a, T b) { return a / b; }
+  // reciprocal-based quotient (2 ulp): the FP32 form trades the IEEE
+  // division sequence for two instructions; its distance to FP64 is reported
+  static __device__ __forceinline__ T div(T a, T b) { return __fdividef(a, b); }
   static __device__ __forceinline__ T fma(T a, T b, T c) { return fmaf(a, b, c); }
   static __device__ __forceinline__ T divu(T x, T, T rc) { return x * rc; }
   static __device__ __forceinline__ T sadd(T a, T b) { return a + b; }
