@@ -369,18 +369,24 @@ __device__ __forceinline__ int ring_slot(int z, int p) {
   return r < 0 ? r + p : r;
 }
 
-template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY>
+template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY, bool TMA>
 __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ FgbLaunch L) {
   using T = typename M::T;
   constexpr int NF = Prog::kFields;
   constexpr int R = Prog::kReach;
   constexpr int H = K * R;
   constexpr int P = 2 * R + 1;
+  constexpr int D = TMA ? 2 : 0;            // input planes in flight ahead of the current one
+  constexpr int P0 = P + D;                 // slots of the input ring
   constexpr int RY = TY + 2 * H, RX = TX + 2 * H;
   constexpr int PL = NF * RY * RX;          // one plane of every field
-  extern __shared__ __align__(16) unsigned char fgb_smem_raw[];
-  T* rings = reinterpret_cast<T*>(fgb_smem_raw);   // [K][P][NF][RY][RX]
+  static_assert(K >= 2, "the input ring is refilled after level 1 has read it");
   static_assert(Prog::kShift >= 0, "the per-step roll is non-negative");
+  extern __shared__ __align__(16) unsigned char fgb_smem_raw[];
+  // input ring [P0][NF][RY][RX], then the rings of levels 1..K-1 [P][NF][RY][RX];
+  // TMA destinations start on 128-byte boundaries
+  const uint32_t base = (uint32_t)__cvta_generic_to_shared(fgb_smem_raw);
+  T* ring0 = reinterpret_cast<T*>(fgb_smem_raw + (TMA ? ((128u - (base & 127u)) & 127u) : 0u));
   const int nz = L.n[0], ny = L.n[1], nx = L.n[2];
   const int x0 = blockIdx.x * TX, y0 = blockIdx.y * TY;
   // the streamed axis is cut into gridDim.z chunks of planes [z0, z1)
@@ -391,72 +397,21 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
   const bool small = TY + H >= ny || TX + H >= nx || H >= nz || K * Prog::kShift >= nx ||
                      K * Prog::kShift >= ny || K * Prog::kShift >= nz;
 
-  // Input planes run over [z0 - H, z1 + H); level t works on plane
-  // zin - t*R.  The next input plane is fetched into registers while the
-  // levels of the current one are computed, so its HBM latency is hidden.
-  constexpr int NI = (RY + BY - 1) / BY, NJ = (RX + BX - 1) / BX;
-  static_assert(K >= 2, "the level-0 ring is refilled after level 1 has read it");
-  T pre[NI][NJ][NF];
-  // the in-plane offsets of this thread's elements do not change from plane
-  // to plane: wrap them once (-1 marks an element outside the tile)
-  int yx[NI][NJ];
-#pragma unroll
-  for (int i = 0; i < NI; ++i) {
-    const int ly = threadIdx.y + i * BY;
-    const int gy = small ? pmod(y0 - H + ly, ny) : pwrap(y0 - H + ly, ny);
-#pragma unroll
-    for (int j = 0; j < NJ; ++j) {
-      const int lx = threadIdx.x + j * BX;
-      const int gx = small ? pmod(x0 - H + lx, nx) : pwrap(x0 - H + lx, nx);
-      yx[i][j] = (ly < RY && lx < RX) ? gy * nx + gx : -1;
-    }
-  }
-  const size_t plane_cells = (size_t)ny * nx;
-  auto fetch = [&](int zin) {
-    const size_t gz = (size_t)(small ? pmod(zin, nz) : pwrap(zin, nz)) * plane_cells;
-#pragma unroll
-    for (int i = 0; i < NI; ++i) {
-#pragma unroll
-      for (int j = 0; j < NJ; ++j) {
-        if (yx[i][j] >= 0) {
-          const size_t g = gz + (size_t)yx[i][j];
-#pragma unroll
-          for (int f = 0; f < NF; ++f)
-            pre[i][j][f] = Storage<S, T>::load(static_cast<const S*>(L.in[f])[g], L.scale[f]);
-        }
-      }
-    }
-  };
-  auto put = [&](int zin) {
-    T* dst = rings + ring_slot(zin, P) * PL + threadIdx.y * RX + threadIdx.x;
-#pragma unroll
-    for (int i = 0; i < NI; ++i) {
-#pragma unroll
-      for (int j = 0; j < NJ; ++j) {
-        if (yx[i][j] >= 0) {
-#pragma unroll
-          for (int f = 0; f < NF; ++f) dst[f * RY * RX + i * BY * RX + j * BX] = pre[i][j][f];
-        }
-      }
-    }
-  };
-  fetch(z0 - H);
-  put(z0 - H);
-  __syncthreads();
-  for (int zin = z0 - H; zin < z1 + H; ++zin) {
-    const bool more = zin + 1 < z1 + H;
-    if (more) fetch(zin + 1);
+  // Levels 1..K of input plane zin: level t works on plane zin - t*R from
+  // the 2R+1 planes around it in the ring of level t-1.
+  auto levels = [&](int zin) {
 #pragma unroll 1
     for (int t = 1; t <= K; ++t) {
       const int zt = zin - t * R;
       if (zt < z0 - (K - t) * R) break;   // this level has nothing to compute yet
-      const T* below = rings + (size_t)(t - 1) * P * PL;
+      const T* below = t == 1 ? ring0 : ring0 + (size_t)P0 * PL + (size_t)(t - 2) * P * PL;
+      const int nslot = t == 1 ? P0 : P;
       const T* planes[P];
 #pragma unroll
-      for (int j = 0; j < P; ++j) planes[j] = below + ring_slot(zt - R + j, P) * PL;
+      for (int j = 0; j < P; ++j) planes[j] = below + ring_slot(zt - R + j, nslot) * PL;
       const int lo = t * R;
       if (t < K) {
-        T* mine = rings + (size_t)t * P * PL + ring_slot(zt, P) * PL;
+        T* mine = ring0 + (size_t)P0 * PL + (size_t)(t - 1) * P * PL + ring_slot(zt, P) * PL;
         for (int ly = lo + threadIdx.y; ly < RY - lo; ly += BY) {
           for (int lx = lo + threadIdx.x; lx < RX - lo; lx += BX) {
             T res[NF];
@@ -489,24 +444,144 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
         }
       }
     }
+  };
+  const int zfirst = z0 - H, zend = z1 + H;   // input planes [zfirst, zend)
+
+  if constexpr (TMA) {
+    static_assert(RX == FGB_TMA_BOX && RY == FGB_TMA_BOX3_Y, "the tensor maps' box is one plane of the tile");
+    static_assert(std::is_same<S, T>::value && (H * sizeof(T)) % 16 == 0 && (TX * sizeof(T)) % 16 == 0,
+                  "box starts on a 16-byte boundary");
+    if (L.tmap != nullptr && x0 >= H && y0 >= H && x0 + TX + H <= nx && y0 + TY + H <= ny) {
+      // Tiles whose halo is inside the grid in x and y stream their input
+      // planes by TMA: plane z goes to ring slot z mod P0 and completes on
+      // that slot's mbarrier; D planes are in flight ahead of the current one.
+      __shared__ __align__(8) uint64_t bars[P0];
+      const bool leader = threadIdx.x == 0 && threadIdx.y == 0;
+      if (leader) {
+#pragma unroll
+        for (int j = 0; j < P0; ++j)
+          asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"((uint32_t)__cvta_generic_to_shared(&bars[j]))
+                       : "memory");
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+      }
+      __syncthreads();
+      auto issue = [&](int z) {   // by the leader
+        const int slot = ring_slot(z, P0);
+        const int gz = small ? pmod(z, nz) : pwrap(z, nz);
+        const uint32_t b = (uint32_t)__cvta_generic_to_shared(&bars[slot]);
+        asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+        asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(b),
+                     "r"((uint32_t)(PL * sizeof(T)))
+                     : "memory");
+#pragma unroll
+        for (int f = 0; f < NF; ++f) {
+          const char* map = static_cast<const char*>(L.tmap) + f * FGB_TMA_MAP_BYTES;
+          const uint32_t dst = (uint32_t)__cvta_generic_to_shared(ring0 + slot * PL + f * RY * RX);
+          asm volatile(
+              "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
+              "%4}], [%5];" ::"r"(dst),
+              "l"(map), "r"(x0 - H), "r"(y0 - H), "r"(gz), "r"(b)
+              : "memory");
+        }
+      };
+      if (leader)
+        for (int d = 0; d < D && zfirst + d < zend; ++d) issue(zfirst + d);
+      for (int zin = zfirst; zin < zend; ++zin) {
+        if (leader && zin + D < zend) issue(zin + D);
+        // wait (bounded) for plane zin: the k-th use of a slot completes phase k
+        const uint32_t b = (uint32_t)__cvta_generic_to_shared(&bars[ring_slot(zin, P0)]);
+        const uint32_t parity = (uint32_t)((zin - zfirst) / P0) & 1u;
+        uint32_t done = 0;
+        for (int it = 0; it < (1 << 20) && !done; ++it)
+          asm volatile(
+              "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
+              : "=r"(done)
+              : "r"(b), "r"(parity)
+              : "memory");
+        if (!__syncthreads_and(done != 0)) {
+          if (leader && L.err) atomicExch(L.err, 2);
+          return;
+        }
+        levels(zin);
+        __syncthreads();
+      }
+      return;
+    }
+  }
+
+  // Ordinary loads: the next input plane is fetched into registers while
+  // the levels of the current one are computed, so its HBM latency is hidden.
+  constexpr int NI = (RY + BY - 1) / BY, NJ = (RX + BX - 1) / BX;
+  T pre[NI][NJ][NF];
+  // the in-plane offsets of this thread's elements do not change from plane
+  // to plane: wrap them once (-1 marks an element outside the tile)
+  int yx[NI][NJ];
+#pragma unroll
+  for (int i = 0; i < NI; ++i) {
+    const int ly = threadIdx.y + i * BY;
+    const int gy = small ? pmod(y0 - H + ly, ny) : pwrap(y0 - H + ly, ny);
+#pragma unroll
+    for (int j = 0; j < NJ; ++j) {
+      const int lx = threadIdx.x + j * BX;
+      const int gx = small ? pmod(x0 - H + lx, nx) : pwrap(x0 - H + lx, nx);
+      yx[i][j] = (ly < RY && lx < RX) ? gy * nx + gx : -1;
+    }
+  }
+  const size_t plane_cells = (size_t)ny * nx;
+  auto fetch = [&](int zin) {
+    const size_t gz = (size_t)(small ? pmod(zin, nz) : pwrap(zin, nz)) * plane_cells;
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        if (yx[i][j] >= 0) {
+          const size_t g = gz + (size_t)yx[i][j];
+#pragma unroll
+          for (int f = 0; f < NF; ++f)
+            pre[i][j][f] = Storage<S, T>::load(static_cast<const S*>(L.in[f])[g], L.scale[f]);
+        }
+      }
+    }
+  };
+  auto put = [&](int zin) {
+    T* dst = ring0 + ring_slot(zin, P0) * PL + threadIdx.y * RX + threadIdx.x;
+#pragma unroll
+    for (int i = 0; i < NI; ++i) {
+#pragma unroll
+      for (int j = 0; j < NJ; ++j) {
+        if (yx[i][j] >= 0) {
+#pragma unroll
+          for (int f = 0; f < NF; ++f) dst[f * RY * RX + i * BY * RX + j * BX] = pre[i][j][f];
+        }
+      }
+    }
+  };
+  fetch(zfirst);
+  put(zfirst);
+  __syncthreads();
+  for (int zin = zfirst; zin < zend; ++zin) {
+    const bool more = zin + 1 < zend;
+    if (more) fetch(zin + 1);
+    levels(zin);
     // level 1 has read the ring slot that plane zin + 1 takes over
     if (more) put(zin + 1);
     __syncthreads();
   }
 }
 
-template <class Prog, int P, class Stage, int TX, int TY, int K>
+template <class Prog, int P, class Stage, int TX, int TY, int K, bool TMA = false>
 struct Tb3dVariant {
   using M = typename Precision<P>::M;
   using S = typename Precision<P>::S;
   using T = typename M::T;
   static constexpr int BX = 32, BY = 8;
   static constexpr int H = K * Prog::kReach;
+  static constexpr int Q = 2 * Prog::kReach + 1;   // slots per ring
   static constexpr size_t kSmem =
-      (size_t)K * (2 * Prog::kReach + 1) * Prog::kFields * (TY + 2 * H) * (TX + 2 * H) * sizeof(T);
+      (size_t)(K * Q + (TMA ? 2 : 0)) * Prog::kFields * (TY + 2 * H) * (TX + 2 * H) * sizeof(T) + (TMA ? 128 : 0);
 
   static cudaError_t launch(const FgbLaunch* L, cudaStream_t stream) {
-    auto kern = tb3d_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY>;
+    auto kern = tb3d_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY, TMA>;
     static bool configured = false;
     if (!configured) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);

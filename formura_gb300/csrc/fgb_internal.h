@@ -22,13 +22,15 @@ struct FgbLaunch {
   float inv_scale[FGB_MAX_FIELDS];
   int n[3];                         // grid extent, leading axes padded with 1
   int fused_steps;                  // >1: temporal blocking inside one launch
-  // 2D grids in FP64/FP32 storage: one TMA tensor map per field of `in`
-  // (box FGB_TMA_BOX x FGB_TMA_BOX elements, device memory), or null
+  // 2D and 3D grids in FP64/FP32 storage: one TMA tensor map per field of
+  // `in` (device memory; boxes of FGB_TMA_BOX x FGB_TMA_BOX elements in 2D,
+  // one plane of FGB_TMA_BOX x FGB_TMA_BOX3_Y in 3D), or null
   const void* tmap;
   int* err;                         // set by a kernel whose bounded wait ran out
 };
 
-#define FGB_TMA_BOX 64
+#define FGB_TMA_BOX 64        // 2D box: 64 x 64; 3D box: 64 x FGB_TMA_BOX3_Y x 1
+#define FGB_TMA_BOX3_Y 32
 #define FGB_TMA_MAP_BYTES 128
 
 #define FGB_MAX_FUSED 8

@@ -152,15 +152,17 @@ static void fill_launch(const fgb_grid* g, int cur, FgbLaunch* L) {
   L->err = g->err;
 }
 
-// TMA tensor maps of the two state buffers (2D, FP64/FP32 storage, rows of a
-// multiple of 16 bytes): boxes of FGB_TMA_BOX^2 elements for the tile kernels.
-// Without them (other grids, or no driver entry point) the kernels load
-// their tiles with ordinary loads.
+// TMA tensor maps of the two state buffers (2D or 3D, FP64/FP32 storage,
+// rows of a multiple of 16 bytes): boxes of FGB_TMA_BOX^2 elements for the 2D
+// tile kernels, planes of FGB_TMA_BOX x FGB_TMA_BOX3_Y for the 3D streaming
+// kernels.  Without them (other grids, or no driver entry point) the
+// kernels load their tiles with ordinary loads.
 static void make_tensor_maps(fgb_grid* g) {
   const FgbProgramDesc* d = g->prog;
   const size_t es = storage_size(g->precision);
-  if (d->dim != 2 || g->precision > FGB_F32 || (g->n[2] * es) % 16 != 0 || g->n[2] < FGB_TMA_BOX ||
-      g->n[1] < FGB_TMA_BOX)
+  const int boxy = d->dim == 3 ? FGB_TMA_BOX3_Y : FGB_TMA_BOX;
+  if (d->dim < 2 || g->precision > FGB_F32 || (g->n[2] * es) % 16 != 0 || g->n[2] < FGB_TMA_BOX ||
+      g->n[1] < boxy)
     return;
   static_assert(sizeof(CUtensorMap) == FGB_TMA_MAP_BYTES, "tensor map size");
   void* fn = nullptr;
@@ -173,15 +175,16 @@ static void make_tensor_maps(fgb_grid* g) {
                                               CUtensorMapInterleave, CUtensorMapSwizzle, CUtensorMapL2promotion,
                                               CUtensorMapFloatOOBfill)>(fn);
   std::vector<CUtensorMap> maps(2 * d->nfields);
-  const cuuint64_t dims[2] = {(cuuint64_t)g->n[2], (cuuint64_t)g->n[1]};
-  const cuuint64_t strides[1] = {(cuuint64_t)g->n[2] * es};
-  const cuuint32_t box[2] = {FGB_TMA_BOX, FGB_TMA_BOX};
-  const cuuint32_t unit[2] = {1, 1};
+  const cuuint32_t rank = (cuuint32_t)d->dim;
+  const cuuint64_t dims[3] = {(cuuint64_t)g->n[2], (cuuint64_t)g->n[1], (cuuint64_t)g->n[0]};
+  const cuuint64_t strides[2] = {(cuuint64_t)g->n[2] * es, (cuuint64_t)g->n[2] * g->n[1] * es};
+  const cuuint32_t box[3] = {FGB_TMA_BOX, (cuuint32_t)boxy, 1};
+  const cuuint32_t unit[3] = {1, 1, 1};
   const CUtensorMapDataType type = es == 8 ? CU_TENSOR_MAP_DATA_TYPE_FLOAT64 : CU_TENSOR_MAP_DATA_TYPE_FLOAT32;
   for (int b = 0; b < 2; ++b)
     for (int f = 0; f < d->nfields; ++f) {
       void* base = (char*)g->state[b] + f * g->cells * es;
-      if (encode(&maps[b * d->nfields + f], type, 2, base, dims, strides, box, unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
+      if (encode(&maps[b * d->nfields + f], type, rank, base, dims, strides, box, unit, CU_TENSOR_MAP_INTERLEAVE_NONE,
                  CU_TENSOR_MAP_SWIZZLE_NONE, CU_TENSOR_MAP_L2_PROMOTION_L2_128B,
                  CU_TENSOR_MAP_FLOAT_OOB_FILL_NONE) != CUDA_SUCCESS)
         return;
@@ -202,7 +205,7 @@ static int check_device_flag(fgb_grid* g) {
   FGB_CUDA(cudaMemcpy(&v, g->err, sizeof v, cudaMemcpyDeviceToHost), "device flag");
   if (v == 0) return FGB_OK;
   cudaMemset(g->err, 0, sizeof(int));
-  return fail(FGB_E_CUDA, "a tile kernel's wait for its TMA load ran out (flag %d)", v);
+  return fail(FGB_E_CUDA, "a %s tile kernel's wait for its TMA load ran out", v == 2 ? "3D" : "2D");
 }
 
 static int run_steps(fgb_grid* g, int nsteps) {

@@ -391,7 +391,8 @@ struct FusedFill {
           Tb3dVariant<Prog, P, Stage0, 64 - 4 * R, 16, 2>::describe(),
           Tb3dVariant<Prog, P, Stage0, 64 - 8 * R, 24, 4>::describe(),
           Tb3dVariant<Prog, P, Stage0, 64 - 8 * R, 16, 4>::describe(),
-          Tb3dVariant<Prog, P, Stage0, 128 - 8 * R, 16, 4>::describe(),
+          // planes arrive by TMA where the tile's halo is inside the grid
+          Tb3dVariant<Prog, P, Stage0, 64 - 8 * R, 32 - 8 * R, 4, R == 1 && P <= 2>::describe(),
           Tb3dVariant<Prog, P, Stage0, 64 - 4 * R, 24, 2>::describe(),
           Tb3dVariant<Prog, P, Stage0, 64 - 16 * R, 16, 8>::describe(),
       };

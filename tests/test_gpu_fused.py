@@ -76,7 +76,7 @@ def test_f16_fused_close_to_f32():
         assert W.rel_l2(fb[i], fa[i]) < 2e-2
 
 
-@pytest.mark.parametrize("shape", [(48, 48, 48), (40, 50, 70), (8, 40, 36), (96, 20, 130)])
+@pytest.mark.parametrize("shape", [(48, 48, 48), (40, 50, 70), (8, 40, 36), (96, 20, 130), (40, 72, 128)])
 @pytest.mark.parametrize("prec", ["f64", "f32"])
 def test_3d_streaming_variants_match_single_steps(shape, prec):
     """The 2.5D streaming kernels (K steps per launch, planes of the slowest
