@@ -172,9 +172,9 @@ __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ F
   bool loaded = false;
   if constexpr (TMA) {
     static_assert(RX == FGB_TMA_BOX && RY == FGB_TMA_BOX, "the tensor maps' box is the tile with its halo");
-    static_assert(std::is_same<S, T>::value && (H * sizeof(T)) % 16 == 0 && (TX * sizeof(T)) % 16 == 0,
+    static_assert(std::is_same<S, T>::value && (HX * sizeof(T)) % 16 == 0 && (TX * sizeof(T)) % 16 == 0,
                   "box starts on a 16-byte boundary");
-    if (L.tmap != nullptr && x0 >= H && y0 >= H && x0 + TX + H <= nx && y0 + TY + H <= ny) {
+    if (L.tmap != nullptr && x0 >= HX && y0 >= HX && x0 + TX + HX <= nx && y0 + TY + HX <= ny) {
       if (!tma_load_tile<T, NF, PLANE>(L, smem, x0 - H, y0 - H)) return;
       loaded = true;
     }
@@ -369,16 +369,20 @@ __device__ __forceinline__ int ring_slot(int z, int p) {
   return r < 0 ? r + p : r;
 }
 
-template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY, bool TMA>
+// HX is the tile's halo in x and y: at least K*R, and wider where that puts
+// the TMA box on a 16-byte boundary (the extra points are loaded and
+// computed but never stored).
+template <class M, class S, class Prog, class Stage, int TX, int TY, int K, int BX, int BY, bool TMA, int HX>
 __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ FgbLaunch L) {
   using T = typename M::T;
   constexpr int NF = Prog::kFields;
   constexpr int R = Prog::kReach;
-  constexpr int H = K * R;
+  constexpr int H = K * R;                  // halo along the streamed axis
+  static_assert(HX >= H, "the tile halo covers K steps");
   constexpr int P = 2 * R + 1;
   constexpr int D = TMA ? 2 : 0;            // input planes in flight ahead of the current one
   constexpr int P0 = P + D;                 // slots of the input ring
-  constexpr int RY = TY + 2 * H, RX = TX + 2 * H;
+  constexpr int RY = TY + 2 * HX, RX = TX + 2 * HX;
   constexpr int PL = NF * RY * RX;          // one plane of every field
   static_assert(K >= 2, "the input ring is refilled after level 1 has read it");
   static_assert(Prog::kShift >= 0, "the per-step roll is non-negative");
@@ -394,7 +398,7 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
   const int z0 = blockIdx.z * zc, z1 = min(nz, z0 + zc);
   if (z0 >= z1) return;
   const T* __restrict__ U = static_cast<const T*>(L.uniforms);
-  const bool small = TY + H >= ny || TX + H >= nx || H >= nz || K * Prog::kShift >= nx ||
+  const bool small = TY + HX >= ny || TX + HX >= nx || H >= nz || K * Prog::kShift >= nx ||
                      K * Prog::kShift >= ny || K * Prog::kShift >= nz;
 
   // Levels 1..K of input plane zin: level t works on plane zin - t*R from
@@ -434,7 +438,7 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
             if (px >= nx) break;
             const int ox = small ? (px + K * Prog::kShift) % nx : pwrap(px + K * Prog::kShift, nx);
             T res[NF];
-            PlaneAccess<T, NF, P, RY, RX> a{planes, (ty + H) * RX + tx + H, res};
+            PlaneAccess<T, NF, P, RY, RX> a{planes, (ty + HX) * RX + tx + HX, res};
             Stage::template run<M>(a, U);
             const size_t g = ((size_t)oz * ny + oy) * nx + ox;
 #pragma unroll
@@ -449,9 +453,9 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
 
   if constexpr (TMA) {
     static_assert(RX == FGB_TMA_BOX && RY == FGB_TMA_BOX3_Y, "the tensor maps' box is one plane of the tile");
-    static_assert(std::is_same<S, T>::value && (H * sizeof(T)) % 16 == 0 && (TX * sizeof(T)) % 16 == 0,
+    static_assert(std::is_same<S, T>::value && (HX * sizeof(T)) % 16 == 0 && (TX * sizeof(T)) % 16 == 0,
                   "box starts on a 16-byte boundary");
-    if (L.tmap != nullptr && x0 >= H && y0 >= H && x0 + TX + H <= nx && y0 + TY + H <= ny) {
+    if (L.tmap != nullptr && x0 >= HX && y0 >= HX && x0 + TX + HX <= nx && y0 + TY + HX <= ny) {
       // Tiles whose halo is inside the grid in x and y stream their input
       // planes by TMA: plane z goes to ring slot z mod P0 and completes on
       // that slot's mbarrier; D planes are in flight ahead of the current one.
@@ -480,7 +484,7 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
           asm volatile(
               "cp.async.bulk.tensor.3d.shared::cluster.global.tile.mbarrier::complete_tx::bytes [%0], [%1, {%2, %3, "
               "%4}], [%5];" ::"r"(dst),
-              "l"(map), "r"(x0 - H), "r"(y0 - H), "r"(gz), "r"(b)
+              "l"(map), "r"(x0 - HX), "r"(y0 - HX), "r"(gz), "r"(b)
               : "memory");
         }
       };
@@ -519,11 +523,11 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
 #pragma unroll
   for (int i = 0; i < NI; ++i) {
     const int ly = threadIdx.y + i * BY;
-    const int gy = small ? pmod(y0 - H + ly, ny) : pwrap(y0 - H + ly, ny);
+    const int gy = small ? pmod(y0 - HX + ly, ny) : pwrap(y0 - HX + ly, ny);
 #pragma unroll
     for (int j = 0; j < NJ; ++j) {
       const int lx = threadIdx.x + j * BX;
-      const int gx = small ? pmod(x0 - H + lx, nx) : pwrap(x0 - H + lx, nx);
+      const int gx = small ? pmod(x0 - HX + lx, nx) : pwrap(x0 - HX + lx, nx);
       yx[i][j] = (ly < RY && lx < RX) ? gy * nx + gx : -1;
     }
   }
@@ -569,7 +573,7 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
   }
 }
 
-template <class Prog, int P, class Stage, int TX, int TY, int K, bool TMA = false>
+template <class Prog, int P, class Stage, int TX, int TY, int K, bool TMA = false, int HX = K * Prog::kReach>
 struct Tb3dVariant {
   using M = typename Precision<P>::M;
   using S = typename Precision<P>::S;
@@ -578,10 +582,10 @@ struct Tb3dVariant {
   static constexpr int H = K * Prog::kReach;
   static constexpr int Q = 2 * Prog::kReach + 1;   // slots per ring
   static constexpr size_t kSmem =
-      (size_t)(K * Q + (TMA ? 2 : 0)) * Prog::kFields * (TY + 2 * H) * (TX + 2 * H) * sizeof(T) + (TMA ? 128 : 0);
+      (size_t)(K * Q + (TMA ? 2 : 0)) * Prog::kFields * (TY + 2 * HX) * (TX + 2 * HX) * sizeof(T) + (TMA ? 128 : 0);
 
   static cudaError_t launch(const FgbLaunch* L, cudaStream_t stream) {
-    auto kern = tb3d_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY, TMA>;
+    auto kern = tb3d_kernel<M, S, Prog, Stage, TX, TY, K, BX, BY, TMA, HX>;
     static bool configured = false;
     if (!configured) {
       cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSmem);

@@ -392,7 +392,8 @@ struct FusedFill {
           Tb3dVariant<Prog, P, Stage0, 64 - 8 * R, 24, 4>::describe(),
           Tb3dVariant<Prog, P, Stage0, 64 - 8 * R, 16, 4>::describe(),
           // planes arrive by TMA where the tile's halo is inside the grid
-          Tb3dVariant<Prog, P, Stage0, 64 - 8 * R, 32 - 8 * R, 4, R == 1 && P <= 2>::describe(),
+          // (K = 2 with a 4-point halo in x and y, so boxes start aligned)
+          Tb3dVariant<Prog, P, Stage0, 56, 24, 2, R == 1 && P <= 2, R == 1 ? 4 : 2 * R>::describe(),
           Tb3dVariant<Prog, P, Stage0, 64 - 4 * R, 24, 2>::describe(),
           Tb3dVariant<Prog, P, Stage0, 64 - 16 * R, 16, 8>::describe(),
       };
