@@ -172,9 +172,9 @@ __global__ void __launch_bounds__(BX * BY) tb2d_kernel(const __grid_constant__ F
   bool loaded = false;
   if constexpr (TMA) {
     static_assert(RX == FGB_TMA_BOX && RY == FGB_TMA_BOX, "the tensor maps' box is the tile with its halo");
-    static_assert(std::is_same<S, T>::value && (HX * sizeof(T)) % 16 == 0 && (TX * sizeof(T)) % 16 == 0,
+    static_assert(std::is_same<S, T>::value && (H * sizeof(T)) % 16 == 0 && (TX * sizeof(T)) % 16 == 0,
                   "box starts on a 16-byte boundary");
-    if (L.tmap != nullptr && x0 >= HX && y0 >= HX && x0 + TX + HX <= nx && y0 + TY + HX <= ny) {
+    if (L.tmap != nullptr && x0 >= H && y0 >= H && x0 + TX + H <= nx && y0 + TY + H <= ny) {
       if (!tma_load_tile<T, NF, PLANE>(L, smem, x0 - H, y0 - H)) return;
       loaded = true;
     }
