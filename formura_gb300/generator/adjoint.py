@@ -13,9 +13,9 @@ program's own SSA chain (seed 1 at each store).  Terms that do not depend
 on the grid are carried symbolically and folded on the host into the
 uniform table, so a linear stencil (heat) costs one multiply-add per cursor;
 terms that do (the reaction terms of Gray-Scott) are evaluated at ``q - d``
-from the forward state.  The reference has no adjoint (SURVEY 8(b) lists
-``Formura_Backward`` as an extension); the checkpointed gradient of the
-runtime (``fgb_gradient_*``) calls this step.
+from the forward state.  The reference has no adjoint; this is the
+``Formura_Backward`` extension of the generated API, and the checkpointed
+gradient of the runtime (``fgb_gradient_*``) calls this step.
 """
 from __future__ import annotations
 

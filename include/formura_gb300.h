@@ -96,10 +96,11 @@ int fgb_set_variant(fgb_grid* grid, int index);
 int fgb_variant(fgb_grid* grid);
 int fgb_autotune(fgb_grid* grid, int trial_steps, int* chosen);
 
-/* Reverse mode (no counterpart in the reference; SURVEY 8(b) names
- * Formura_Backward as the extension).  The adjoint step is generated from
- * the program's own step function by reverse-mode differentiation
- * (single-stage programs, FP64 and FP32).
+/* Reverse mode (no counterpart in the reference: the Formura_Backward
+ * extension of the generated API).  The adjoint step is generated from the
+ * program's own step function by reverse-mode differentiation: one pass for
+ * single-stage steps, two passes per stage for multi-stage steps (programs
+ * built with gpu_adjoint: 1), in FP64 and FP32.
  *
  * fgb_backward: one adjoint step at the current state u_n:
  *   lambda = (dF/du at u_n)^T lambda_next   (host FP64, formura_data layout).
