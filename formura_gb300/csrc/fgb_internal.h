@@ -106,6 +106,7 @@ struct FgbProgramDesc {
   FgbAdjLaunchFn adj_partial[FGB_NUM_PRECISIONS][FGB_MAX_STAGES];
   FgbAdjLaunchFn adj_gather[FGB_NUM_PRECISIONS][FGB_MAX_STAGES];
   int adj_pairs[FGB_MAX_STAGES];
+  int adj_parts[FGB_MAX_STAGES];   // partial-sum kernels per stage
 };
 
 typedef const FgbProgramDesc* (*FgbProgramGetter)(void);

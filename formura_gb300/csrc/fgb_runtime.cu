@@ -614,7 +614,7 @@ static int stage_adjoint_step(fgb_grid* g, const void* u) {
     cudaError_t e = d->adj_partial[g->precision][s](&A, g->stream);
     if (e == cudaSuccess) e = d->adj_gather[g->precision][s](&A, g->stream);
     if (e != cudaSuccess) return cuda_fail(e, "adjoint launch");
-    g->launches += 2;
+    g->launches += d->adj_parts[s] + 1;
   }
   ++g->grad_adj;
   g->lcur ^= 1;

@@ -457,9 +457,12 @@ struct AdjPartialAccess {
   __device__ __forceinline__ T ldlm() const {
     return ro_load(static_cast<const T*>(L.lmid[K]) + lin(p0, p1, p2));
   }
-  template <int J>
+  // partial sum of pair J: stored by the first kernel of the stage that
+  // reaches it, added to by the others
+  template <int J, bool FIRST>
   __device__ __forceinline__ void stp(T v) const {
-    static_cast<T*>(L.pair[J])[lin(p0, p1, p2)] = v;
+    T* a = static_cast<T*>(L.pair[J]) + lin(p0, p1, p2);
+    *a = FIRST ? v : v + *a;
   }
 };
 
@@ -518,6 +521,20 @@ struct AdjointStagePair {
 };
 template <class... Pairs>
 struct AdjointStages {};
+// the partial-sum kernels of one stage, launched in order
+template <class... Parts>
+struct AdjParts {};
+template <class Prog, int P, class List>
+struct PartialLauncher;
+template <class Prog, int P, class... Parts>
+struct PartialLauncher<Prog, P, AdjParts<Parts...>> {
+  static constexpr int kCount = sizeof...(Parts);
+  static cudaError_t launch(const FgbAdjLaunch* L, cudaStream_t stream) {
+    cudaError_t e = cudaSuccess;
+    ((e = (e == cudaSuccess ? launch_adj_stage<Prog, P, Parts, false>(L, stream) : e)), ...);
+    return e;
+  }
+};
 
 template <class Prog, class A>
 struct StageAdjointFill {
@@ -532,15 +549,17 @@ struct StageAdjointFill<Prog, AdjointStages<Pairs...>> {
   static void fill(FgbProgramDesc& d) {
     static_assert(sizeof...(Pairs) == Prog::kStages, "one adjoint pair per stage");
     const int pairs[] = {Pairs::P1::kPairs...};
-    const FgbAdjLaunchFn p0[] = {&launch_adj_stage<Prog, 0, typename Pairs::P1, false>...};
+    const int parts[] = {PartialLauncher<Prog, 0, typename Pairs::P1::Parts>::kCount...};
+    const FgbAdjLaunchFn p0[] = {&PartialLauncher<Prog, 0, typename Pairs::P1::Parts>::launch...};
     const FgbAdjLaunchFn g0[] = {&launch_adj_stage<Prog, 0, typename Pairs::P2, true>...};
-    const FgbAdjLaunchFn p2[] = {&launch_adj_stage<Prog, 2, typename Pairs::P1, false>...};
+    const FgbAdjLaunchFn p2[] = {&PartialLauncher<Prog, 2, typename Pairs::P1::Parts>::launch...};
     const FgbAdjLaunchFn g2[] = {&launch_adj_stage<Prog, 2, typename Pairs::P2, true>...};
     for (int p = 0; p < FGB_NUM_PRECISIONS; ++p)
       for (int s = 0; s < FGB_MAX_STAGES; ++s) d.adj_partial[p][s] = d.adj_gather[p][s] = nullptr;
     static_assert(((Pairs::P1::kPairs <= FGB_MAX_PAIRS) && ...), "too many (array, cursor) pairs in a stage");
     for (int s = 0; s < (int)sizeof...(Pairs); ++s) {
       d.adj_pairs[s] = pairs[s];
+      d.adj_parts[s] = parts[s];
       d.adj_partial[0][s] = p0[s];
       d.adj_gather[0][s] = g0[s];
       d.adj_partial[2][s] = p2[s];

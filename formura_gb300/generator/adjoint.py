@@ -276,18 +276,38 @@ def _as_alg(h):
     return h
 
 
+def _stage_outputs(st) -> List[tuple]:
+    """The outputs of a stage in emission order: ('s', node) for a store of
+    the new state, ('m', node) for a manifest array kept in HBM."""
+    out = []
+    for node in st.nodes:
+        if node.is_store:
+            out.append(("s", node))
+        if node.omid in st.mid_out:
+            out.append(("m", node))
+    return out
+
+
+# a partial-sum kernel holds the forward values of its outputs' backward
+# slice in registers: stages larger than this many micro operations are cut
+# into several kernels by output, so that none of them spills
+_PARTIAL_MICRO_OPS = 1000
+
+
 def emit_stage_adjoints(pe: _ProgramEmitter):
-    """Adjoint of a step made of several stages (HLLC, HLLD), as two functors
-    per stage.
+    """Adjoint of a step made of several stages (HLLC, HLLD), as partial-sum
+    functors and one gather functor per stage.
 
     Stage s computes its outputs o (manifest arrays, or the new state) at p
     from its inputs x (state fields and earlier arrays) read at p + c.  With
     lam_o the adjoint of each output:
 
-    * ``AdjStage<s>`` evaluates the stage forward at p once, seeds the reverse
-      sweep of its SSA chain with lam_o(p) (lam of the new state is read at
-      p + shift, where the forward wrote it) and stores, for every input read
-      (x, c), the partial sum P_(x,c)(p) = sum_o lam_o(p) * do(p)/dx(p + c);
+    * ``AdjStage<s>_<g>`` evaluates the stage forward at p, seeds the reverse
+      sweep of its SSA chain with lam_o(p) for the outputs o of group g (lam
+      of the new state is read at p + shift, where the forward wrote it) and
+      adds, for every input read (x, c), lam_o(p) * do(p)/dx(p + c) to the
+      partial sum P_(x,c)(p); the first group that reaches a pair stores it.
+      Large stages are cut into groups of outputs so that no kernel spills;
     * ``AdjGather<s>`` forms lam_x(q) = sum_c P_(x,c)(q - c) in a fixed order,
       storing it for the first stage (in reverse order) that reads x and
       adding to it for the others.
@@ -302,124 +322,61 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
     fields = pe.fields
     an = pe.an
     shift3 = [pe.shift if i >= 3 - pe.dim else 0 for i in range(3)]
-    pass1: List[str] = []
+    pass1: Dict[int, str] = {}
     pair_lists: List[List[tuple]] = []
     for st in pe.stages:
-        se = _StageEmitter(pe, st)
-        for node in st.nodes:
-            se.node(node)       # the forward at p; its stores are no-ops in the adjoint accessor
-        defs: Dict[tuple, tuple] = {}
-        order: List[tuple] = []
-        for node in st.nodes:
-            for idx, mn in enumerate(node.micro):
-                if mn.key not in defs:
-                    defs[mn.key] = (node, idx)
-                    order.append(mn.key)
-        alg = _Algebra(se, pe)
-        bar: Dict[tuple, List[tuple]] = {}
-        for node in st.nodes:
-            if node.is_store:
-                store = node.micro[-1]
-                f = fields.index(store.inst[1])
-                lam = se.bind(f"a.template ldl<{f}, {shift3[0]}, {shift3[1]}, {shift3[2]}>()")
-                bar.setdefault(node.micro[store.inst[2]].key, []).append(lam)
-            if node.omid in st.mid_out:
-                k = pe.mids.index(node.omid)
-                lam = se.bind(f"a.template ldlm<{k}>()")
-                bar.setdefault(node.micro[-1].key, []).append(lam)
-        pairs: List[tuple] = []
-        pair_val: Dict[tuple, tuple] = {}
-
-        def value(key):
-            return _as_alg(se.var[key])
-
-        for key in reversed(order):
-            if key not in bar:
-                continue
-            node, i = defs[key]
-            micro = node.micro
-            inst = micro[i].inst
-            k = inst[0]
-            total = bar[key][0]
-            for t in bar[key][1:]:
-                total = alg.add(total, t)
-            if k == "loadstatic" or (k == "loadcursor" and stage_of[inst[2]] != st.index):
-                kind = ("s", fields.index(inst[2])) if k == "loadstatic" else ("m", pe.mids.index(inst[2]))
-                pair = kind + (tuple(pe.cursor3(inst[1])),)
-                if pair in pair_val:
-                    pair_val[pair] = alg.add(pair_val[pair], total)
+        texts: List[str] = []
+        outs = _stage_outputs(st)
+        nmicro = sum(len(n.micro) for n in st.nodes)
+        ngroups = max(1, min(len(outs), -(-nmicro // _PARTIAL_MICRO_OPS)))
+        per = -(-len(outs) // ngroups)
+        groups = [outs[i:i + per] for i in range(0, len(outs), per)]
+        pairs: List[tuple] = []           # (x, c) pairs of the stage, in order of first touch
+        part_names: List[str] = []
+        for gi, group in enumerate(groups):
+            se = _StageEmitter(pe, st)
+            for node in st.nodes:
+                se.node(node)   # the forward at p; stores are no-ops, unused values are dropped
+            defs: Dict[tuple, tuple] = {}
+            order: List[tuple] = []
+            for node in st.nodes:
+                for idx, mn in enumerate(node.micro):
+                    if mn.key not in defs:
+                        defs[mn.key] = (node, idx)
+                        order.append(mn.key)
+            alg = _Algebra(se, pe)
+            bar: Dict[tuple, List[tuple]] = {}
+            for kind, node in group:
+                if kind == "s":
+                    store = node.micro[-1]
+                    f = fields.index(store.inst[1])
+                    lam = se.bind(f"a.template ldl<{f}, {shift3[0]}, {shift3[1]}, {shift3[2]}>()")
+                    bar.setdefault(node.micro[store.inst[2]].key, []).append(lam)
                 else:
+                    k = pe.mids.index(node.omid)
+                    lam = se.bind(f"a.template ldlm<{k}>()")
+                    bar.setdefault(node.micro[-1].key, []).append(lam)
+            touched: List[tuple] = []
+            pair_val: Dict[tuple, tuple] = {}
+            _reverse_sweep(se, alg, an, fields, pe, stage_of, st, defs, order, bar, touched, pair_val)
+            for pair in touched:
+                first = pair not in pairs
+                if first:
                     pairs.append(pair)
-                    pair_val[pair] = total
-                continue
-            if k in ("imm", "loadindex", "store", "loadcursor"):
-                continue
-            if an.om_uniform(key[1]):
-                continue
-            Y = total
-
-            def opk(j, micro=micro):
-                return micro[j].key
-
-            def push(j, v, micro=micro):
-                mj = micro[j]
-                if mj.inst[0] in ("loadstatic", "loadcursor") or not an.om_uniform(mj.key[1]):
-                    bar.setdefault(mj.key, []).append(v())
-
-            if k == "uniop":
-                op, a = inst[1], inst[2]
-                if op == "+":
-                    push(a, lambda: Y)
-                elif op == "-":
-                    push(a, lambda: alg.neg(Y))
-                else:
-                    fn = op[len("external-call/"):]
-                    x = alg.T(value(opk(a)))
-                    y = alg.T(value(key))
-                    d = {"sqrt": f"M::div(T(0.5), {y})", "exp": y, "log": f"M::div(T(1), {x})",
-                         "sin": f"M::cos({x})", "cos": f"M::neg(M::sin({x}))",
-                         "fabs": f"({x} < T(0) ? T(-1) : T(1))"}.get(fn)
-                    if d is None:
-                        raise FormuraCompileError(f"no derivative for {fn}")
-                    push(a, lambda: alg.mul(Y, se.bind(d)))
-            elif k == "binop":
-                op, a, b = inst[1], inst[2], inst[3]
-                if op in _CMP:
-                    continue
-                if op == "+":
-                    push(a, lambda: Y)
-                    push(b, lambda: Y)
-                elif op == "-":
-                    push(a, lambda: Y)
-                    push(b, lambda: alg.neg(Y))
-                elif op == "*":
-                    push(a, lambda: alg.mul(Y, value(opk(b))))
-                    push(b, lambda: alg.mul(Y, value(opk(a))))
-                elif op == "/":
-                    push(a, lambda: alg.div(Y, value(opk(b))))
-                    if not an.om_uniform(micro[b].key[1]) or micro[b].inst[0] in ("loadstatic", "loadcursor"):
-                        push(b, lambda: alg.neg(alg.div(alg.mul(Y, value(key)), value(opk(b)))))
-                elif op == "**":
-                    A, B = alg.T(value(opk(a))), alg.T(value(opk(b)))
-                    push(a, lambda: alg.mul(Y, se.bind(f"M::mul({B}, M::pow({A}, M::sub({B}, T(1))))")))
-                    if not an.om_uniform(micro[b].key[1]):
-                        push(b, lambda: alg.mul(Y, se.bind(f"M::mul({alg.T(value(key))}, M::log({A}))")))
-                else:
-                    raise FormuraCompileError(f"no derivative for {op}")
-            elif k == "triop":
-                c, a, b = inst[2], inst[3], inst[4]
-                C = se.as_bool(value(opk(c)))
-                push(a, lambda: se.bind(f"({C} ? {alg.T(Y)} : T(0))"))
-                push(b, lambda: se.bind(f"({C} ? T(0) : {alg.T(Y)})"))
-        for j, pair in enumerate(pairs):
-            se.emit(f"a.template stp<{j}>({alg.T(pair_val[pair])});")
+                j = pairs.index(pair)
+                se.emit(f"a.template stp<{j}, {'true' if first else 'false'}>({alg.T(pair_val[pair])});")
+            body = "\n".join(se.lines)
+            name = f"AdjStage{st.index}_{gi}"
+            part_names.append(name)
+            texts.append(f"struct {name} {{\n"
+                         f"  template <class M, class A>\n"
+                         f"  static __device__ __forceinline__ void run(const A& a, const typename M::U* __restrict__ U) {{\n"
+                         f"    using T = typename M::T;\n    (void)U;\n{body}\n  }}\n}};\n")
         pair_lists.append(pairs)
-        body = "\n".join(se.lines)
-        pass1.append(f"struct AdjStage{st.index} {{\n"
+        texts.append(f"struct AdjStage{st.index} {{\n"
                      f"  static constexpr int kPairs = {len(pairs)};\n"
-                     f"  template <class M, class A>\n"
-                     f"  static __device__ __forceinline__ void run(const A& a, const typename M::U* __restrict__ U) {{\n"
-                     f"    using T = typename M::T;\n    (void)U;\n{body}\n  }}\n}};\n")
+                     f"  using Parts = fgb::AdjParts<{', '.join(part_names)}>;\n}};\n")
+        pass1[st.index] = "\n".join(texts)
     # gathers, in the order the adjoint runs them (last stage first)
     written = set()
     gathers: Dict[int, str] = {}
@@ -451,3 +408,91 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
     pairs_list = ", ".join(f"fgb::AdjointStagePair<AdjStage{s}, AdjGather{s}>" for s in range(S))
     src += f"using StageAdjointList = fgb::AdjointStages<{pairs_list}>;\n"
     return src, pair_lists
+
+
+def _reverse_sweep(se, alg, an, fields, pe, stage_of, st, defs, order, bar, touched, pair_val):
+    """Reverse sweep of one stage's SSA chain from the seeds in `bar`:
+    appends the (input array, cursor) pairs reached to `touched` and their
+    summed adjoints to `pair_val`."""
+
+    def value(key):
+        return _as_alg(se.var[key])
+
+    for key in reversed(order):
+        if key not in bar:
+            continue
+        node, i = defs[key]
+        micro = node.micro
+        inst = micro[i].inst
+        k = inst[0]
+        total = bar[key][0]
+        for t in bar[key][1:]:
+            total = alg.add(total, t)
+        if k == "loadstatic" or (k == "loadcursor" and stage_of[inst[2]] != st.index):
+            kind = ("s", fields.index(inst[2])) if k == "loadstatic" else ("m", pe.mids.index(inst[2]))
+            pair = kind + (tuple(pe.cursor3(inst[1])),)
+            if pair in pair_val:
+                pair_val[pair] = alg.add(pair_val[pair], total)
+            else:
+                touched.append(pair)
+                pair_val[pair] = total
+            continue
+        if k in ("imm", "loadindex", "store", "loadcursor"):
+            continue
+        if an.om_uniform(key[1]):
+            continue
+        Y = total
+
+        def opk(j, micro=micro):
+            return micro[j].key
+
+        def push(j, v, micro=micro):
+            mj = micro[j]
+            if mj.inst[0] in ("loadstatic", "loadcursor") or not an.om_uniform(mj.key[1]):
+                bar.setdefault(mj.key, []).append(v())
+
+        if k == "uniop":
+            op, a = inst[1], inst[2]
+            if op == "+":
+                push(a, lambda: Y)
+            elif op == "-":
+                push(a, lambda: alg.neg(Y))
+            else:
+                fn = op[len("external-call/"):]
+                x = alg.T(value(opk(a)))
+                y = alg.T(value(key))
+                d = {"sqrt": f"M::div(T(0.5), {y})", "exp": y, "log": f"M::div(T(1), {x})",
+                     "sin": f"M::cos({x})", "cos": f"M::neg(M::sin({x}))",
+                     "fabs": f"({x} < T(0) ? T(-1) : T(1))"}.get(fn)
+                if d is None:
+                    raise FormuraCompileError(f"no derivative for {fn}")
+                push(a, lambda: alg.mul(Y, se.bind(d)))
+        elif k == "binop":
+            op, a, b = inst[1], inst[2], inst[3]
+            if op in _CMP:
+                continue
+            if op == "+":
+                push(a, lambda: Y)
+                push(b, lambda: Y)
+            elif op == "-":
+                push(a, lambda: Y)
+                push(b, lambda: alg.neg(Y))
+            elif op == "*":
+                push(a, lambda: alg.mul(Y, value(opk(b))))
+                push(b, lambda: alg.mul(Y, value(opk(a))))
+            elif op == "/":
+                push(a, lambda: alg.div(Y, value(opk(b))))
+                if not an.om_uniform(micro[b].key[1]) or micro[b].inst[0] in ("loadstatic", "loadcursor"):
+                    push(b, lambda: alg.neg(alg.div(alg.mul(Y, value(key)), value(opk(b)))))
+            elif op == "**":
+                A, B = alg.T(value(opk(a))), alg.T(value(opk(b)))
+                push(a, lambda: alg.mul(Y, se.bind(f"M::mul({B}, M::pow({A}, M::sub({B}, T(1))))")))
+                if not an.om_uniform(micro[b].key[1]):
+                    push(b, lambda: alg.mul(Y, se.bind(f"M::mul({alg.T(value(key))}, M::log({A}))")))
+            else:
+                raise FormuraCompileError(f"no derivative for {op}")
+        elif k == "triop":
+            c, a, b = inst[2], inst[3], inst[4]
+            C = se.as_bool(value(opk(c)))
+            push(a, lambda: se.bind(f"({C} ? {alg.T(Y)} : T(0))"))
+            push(b, lambda: se.bind(f"({C} ? T(0) : {alg.T(Y)})"))

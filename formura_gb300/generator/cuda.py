@@ -340,6 +340,7 @@ class _StageEmitter:
         self.n = 0
         self.load_fp64 = 0.0                   # balance of the two pipes
         self.load_int = 0.0
+        self.scaled: Dict[tuple, str] = {}     # materialised power-of-two products
 
     def fresh(self) -> str:
         self.n += 1
@@ -362,7 +363,7 @@ class _StageEmitter:
         raise AssertionError(h)
 
     def materialize(self, h) -> str:
-        cache = self.p.scaled_cache.setdefault(id(self), {})
+        cache = self.scaled
         key = (h[1], self.as_T(h[2]))
         if key not in cache:
             name = self.fresh()
@@ -544,7 +545,6 @@ class _ProgramEmitter:
         self.stages = build_stages(self.mmg)
         self.mids = sorted({m for s in self.stages for m in s.mid_out})
         self.table: List[tuple] = []
-        self.scaled_cache: Dict[int, dict] = {}
         self.soft_cost = soft_cost_default()
         self.stage_adjoint = stage_adjoint
         self.adjoint_pairs: List[List[tuple]] = []

@@ -29,6 +29,8 @@ struct AdjointStagePair {
   using P1 = Partial;
   using P2 = Gather;
 };
+template <class... Parts>
+struct AdjParts {};
 }  // namespace fgb
 
 namespace hostshim {
@@ -115,8 +117,11 @@ struct Partial {
   double ldl() const { return g->lnext[F * g->cells + g->lin(p0 + D0, p1 + D1, p2 + D2)]; }
   template <int K>
   double ldlm() const { return g->lmids[K * g->cells + g->lin(p0, p1, p2)]; }
-  template <int J>
-  void stp(double v) const { g->pairs[J * g->cells + g->lin(p0, p1, p2)] = v; }
+  template <int J, bool FIRST>
+  void stp(double v) const {
+    double& a = g->pairs[J * g->cells + g->lin(p0, p1, p2)];
+    a = FIRST ? v : v + a;
+  }
 };
 
 struct Gather {
@@ -160,10 +165,14 @@ struct Runner {
     int s = 0;
     ((s++ < upto ? sweep<FwdAcc, Stages>(g) : void()), ...);
   }
+  template <class... Parts>
+  static void partials(Grid& g, fgb::AdjParts<Parts...>) {
+    (sweep<Partial, Parts>(g), ...);
+  }
   template <class P>
   static void stage_pair(Grid& g, int& most) {
     g.pairs.assign((size_t)P::P1::kPairs * g.cells + 1, 0.0);
-    sweep<Partial, typename P::P1>(g);
+    partials(g, typename P::P1::Parts{});
     sweep<Gather, typename P::P2>(g);
     (void)most;
   }
