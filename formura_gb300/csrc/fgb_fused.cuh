@@ -612,95 +612,4 @@ struct Tb3dVariant {
   }
 };
 
-// One step per launch for 3D programs, marching along the slowest axis: a
-// thread owns one (y, x) column of a chunk of planes and keeps the 2R+1
-// values of that column around the current plane in registers, so a point
-// loads one new value of its own column (the plane R ahead, fetched one
-// plane early) plus its neighbours in the plane, which adjacent threads
-// share through L1.
-template <class S, class T, int NF, int R, int SHIFT>
-struct ColumnAccess {
-  const FgbLaunch& L;
-  const T (*win)[2 * R + 1];   // [field][z - R .. z + R] of this column
-  int p0, p1, p2;
-  __device__ __forceinline__ uint32_t lin(int i0, int i1, int i2) const {
-    return ((uint32_t)i0 * (uint32_t)L.n[1] + (uint32_t)i1) * (uint32_t)L.n[2] + (uint32_t)i2;
-  }
-  template <int F, int D0, int D1, int D2>
-  __device__ __forceinline__ T ld() const {
-    if constexpr (D1 == 0 && D2 == 0) {
-      return win[F][D0 + R];
-    } else {
-      const S* a = static_cast<const S*>(L.in[F]);
-      return Storage<S, T>::load(ro_load(a + lin(wrap<D0>(p0, L.n[0]), wrap<D1>(p1, L.n[1]), wrap<D2>(p2, L.n[2]))),
-                                 L.scale[F]);
-    }
-  }
-  template <int F>
-  __device__ __forceinline__ void st(T v) const {
-    S* a = static_cast<S*>(L.out[F]);
-    a[lin(wrap<SHIFT>(p0, L.n[0]), wrap<SHIFT>(p1, L.n[1]), wrap<SHIFT>(p2, L.n[2]))] =
-        Storage<S, T>::store(v, L.inv_scale[F]);
-  }
-};
-
-template <class M, class S, class Prog, class Stage, int ZC>
-__global__ void __launch_bounds__(kBlockX) zmarch_kernel(const __grid_constant__ FgbLaunch L) {
-  using T = typename M::T;
-  constexpr int NF = Prog::kFields;
-  constexpr int R = Prog::kReach;
-  constexpr int W = 2 * R + 1;
-  const int nz = L.n[0], ny = L.n[1], nx = L.n[2];
-  const int x = blockIdx.x * blockDim.x + threadIdx.x;
-  if (x >= nx) return;
-  const int y = blockIdx.y;
-  const int z0 = blockIdx.z * ZC, z1 = min(nz, z0 + ZC);
-  const size_t plane = (size_t)ny * nx, col = (size_t)y * nx + x;
-  const T* __restrict__ U = static_cast<const T*>(L.uniforms);
-  auto at = [&](int f, int z) {   // this column's value at plane z (periodic)
-    const int w = pmod(z, nz);
-    return Storage<S, T>::load(ro_load(static_cast<const S*>(L.in[f]) + w * plane + col), L.scale[f]);
-  };
-  T win[NF][W];
-#pragma unroll
-  for (int f = 0; f < NF; ++f)
-#pragma unroll
-    for (int j = 0; j < W; ++j) win[f][j] = at(f, z0 - R + j);
-  for (int z = z0; z < z1; ++z) {
-    T ahead[NF];
-    const bool more = z + 1 < z1;
-#pragma unroll
-    for (int f = 0; f < NF; ++f) ahead[f] = more ? at(f, z + R + 1) : T(0);
-    ColumnAccess<S, T, NF, R, Prog::kShift> a{L, win, z, y, x};
-    Stage::template run<M>(a, U);
-#pragma unroll
-    for (int f = 0; f < NF; ++f) {
-#pragma unroll
-      for (int j = 0; j + 1 < W; ++j) win[f][j] = win[f][j + 1];
-      win[f][W - 1] = ahead[f];
-    }
-  }
-}
-
-template <class Prog, int P, class Stage, int ZC>
-struct Zmarch3dVariant {
-  using M = typename Precision<P>::M;
-  using S = typename Precision<P>::S;
-  static cudaError_t launch(const FgbLaunch* L, cudaStream_t stream) {
-    const int bx = L->n[2] >= kBlockX ? kBlockX : ((L->n[2] + 31) / 32) * 32;
-    dim3 grid((L->n[2] + bx - 1) / bx, L->n[1], (L->n[0] + ZC - 1) / ZC);
-    zmarch_kernel<M, S, Prog, Stage, ZC><<<grid, bx, 0, stream>>>(*L);
-    return cudaGetLastError();
-  }
-  static FgbFusedVariant describe() {
-    FgbFusedVariant v;
-    v.launch = &launch;
-    v.tile_x = kBlockX;
-    v.tile_y = 1;
-    v.steps = 1;
-    v.smem_bytes = 0;
-    return v;
-  }
-};
-
 }  // namespace fgb

@@ -395,8 +395,7 @@ struct FusedFill {
           // (K = 2 with a 4-point halo in x and y, so boxes start aligned)
           Tb3dVariant<Prog, P, Stage0, 56, 24, 2, R == 1 && P <= 2, R == 1 ? 4 : 2 * R>::describe(),
           Tb3dVariant<Prog, P, Stage0, 64 - 4 * R, 24, 2>::describe(),
-          // one step per launch, marching a column along the slowest axis
-          Zmarch3dVariant<Prog, P, Stage0, 32>::describe(),
+          Tb3dVariant<Prog, P, Stage0, 64 - 16 * R, 16, 8>::describe(),
       };
       d.nfused[P] = (int)(sizeof v / sizeof v[0]);
       for (int i = 0; i < d.nfused[P]; ++i) d.fused[P][i] = v[i];
