@@ -145,3 +145,68 @@ def test_generated_adjoint_is_the_transpose(generated, tmp_path_factory, program
     jtw = host.backward(u, w)
     lhs, rhs = float(np.vdot(jv, w)), float(np.vdot(v, jtw))
     assert abs(lhs - rhs) <= 1e-6 * abs(lhs), (lhs, rhs)
+
+
+# ---------------------------------------------------------------------------
+# the reference's own programs through the CUDA emitter (this container only)
+# ---------------------------------------------------------------------------
+REFERENCE_PROGRAMS = {
+    "diffusion1": ("examples/diffusion1/diffusion1.fmr", "examples/diffusion1/diffusion1.yaml", None),
+    "diffusion2": ("examples/diffusion2/diffusion2.fmr", "examples/diffusion2/diffusion2.yaml", None),
+    "diffusion3": ("examples/diffusion3/diffusion3.fmr", "examples/diffusion3/diffusion3.yaml", "[20, 20, 20]"),
+    "pearson2": ("examples/pearson2/pearson2.fmr", "examples/pearson2/pearson2.yaml", "[64, 64]"),
+    "hllc1d": ("sample/1d_hllc/hllc.fmr", "sample/1d_hllc/config.yaml", None),
+    "hllc3d_sample": ("sample/3d_hllc/3d_hllc.fmr", "sample/3d_hllc/config.yaml", "[12, 12, 12]"),
+    "hlld1d": ("sample/mhd_1d_hlld/mhd_hlld.fmr", "sample/mhd_1d_hlld/config.yaml", None),
+    "hlld3d_sample": ("sample/mhd_3d_hlld/mhd_3d_hlld.fmr", "sample/mhd_3d_hlld/config.yaml", "[10, 10, 10]"),
+}
+
+
+def _one_rank_config(text, grid=None):
+    """The sample's config for one rank, one step per Formura_Forward: MPI
+    shape and temporal blocking dropped, optionally a smaller grid."""
+    keep = []
+    for line in text.splitlines():
+        key = line.split(":")[0].strip()
+        if key in ("mpi_shape", "grid_per_block", "temporal_blocking_interval"):
+            continue
+        if key == "grid_per_node" and grid is not None:
+            line = f"grid_per_node: {grid}"
+        keep.append(line)
+    return "\n".join(keep) + "\n"
+
+
+@pytest.mark.parametrize("name", sorted(REFERENCE_PROGRAMS))
+def test_reference_program_through_cuda_emitter(tmp_path, name):
+    """The CUDA emitter's code for the reference's own example and sample
+    programs, run on the host, equals the oracle bit for bit from each
+    program's own initial state."""
+    from formura_gb300.generator.config import decode_config
+    from formura_gb300.generator.cuda import emit_cuda, uniform_table
+    from formura_gb300.generator.manifest import compile_program
+    from conftest import REFERENCE
+    if not os.path.isdir(REFERENCE):
+        pytest.skip("the reference tree is not present")
+    fmr, yml, grid = REFERENCE_PROGRAMS[name]
+    with open(os.path.join(REFERENCE, fmr)) as f:
+        src = f.read()
+    with open(os.path.join(REFERENCE, yml)) as f:
+        cfg = _one_rank_config(f.read(), grid)
+    mm = compile_program(src, decode_config(cfg))
+    kp = emit_cuda(mm, f"ref_{name}", [], stage_adjoint=False)
+    cu = tmp_path / f"ref_{name}.cu"
+    cu.write_text(kp.source)
+    so = str(tmp_path / f"ref_{name}.so")
+    subprocess.check_call(["g++", "-O1", "-std=c++17", "-ffp-contract=off", "-fPIC", "-shared", "-I", SHIM,
+                           "-x", "c++", str(cu), "-o", so])
+    ref = ReferenceProgram(src, cfg, f"refemit_{name}")
+    ref.init()
+    u = np.stack([ref.get(f) for f in ref.fields])
+    shape = u.shape[1:]
+    host = HostProgram(ctypes.CDLL(so), f"ref_{name}", shape, uniform_table(mm, kp))
+    steps = 3
+    ref.forward(steps)
+    for _ in range(steps):
+        u = host.forward(u)
+    for i, f in enumerate(ref.fields):
+        assert np.array_equal(u[i], ref.get(f)), f
