@@ -26,7 +26,7 @@ CSRC = os.path.join(HERE, "csrc")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                     "-Xptxas", "-O3", "--expt-relaxed-constexpr"]
+                     "-Xptxas", "-O3", "--expt-relaxed-constexpr"] + os.environ.get("FGB_NVCC_EXTRA", "").split()
 
 
 def program_names() -> List[str]:
