@@ -26,7 +26,9 @@ CSRC = os.path.join(HERE, "csrc")
 
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 NVCC_FLAGS = ARCH + ["-O3", "-lineinfo", "-std=c++17", "-Xcompiler", "-fPIC",
-                     "-Xptxas", "-O3", "--expt-relaxed-constexpr"] + os.environ.get("FGB_NVCC_EXTRA", "").split()
+                     "-Xptxas", "-O3", "--expt-relaxed-constexpr"]
+# extra nvcc options for experiments (for example -DFGB_DIVU_IEEE)
+NVCC_FLAGS += os.environ.get("FGB_NVCC_EXTRA", "").split()
 
 
 def program_names() -> List[str]:

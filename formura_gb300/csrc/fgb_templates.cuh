@@ -282,16 +282,13 @@ struct AdjointAccess {
 };
 
 constexpr int kBlockX = 128;
-#ifndef FGB_STAGE_MINB
-#define FGB_STAGE_MINB 1
-#endif
 
 // One thread per grid point of RPT consecutive rows (the middle axis); x
 // covers the contiguous (last) axis.  With RPT > 1 a thread has the loads of
 // several points in flight at once, which is what a memory-bound FP32/FP16
 // step needs to cover the HBM latency.
 template <class M, class S, int DIM, int SHIFT, class Stage, int RPT>
-__global__ void __launch_bounds__(kBlockX, RPT > 1 ? FGB_STAGE_MINB : 1) stage_kernel(const __grid_constant__ FgbLaunch L) {
+__global__ void __launch_bounds__(kBlockX) stage_kernel(const __grid_constant__ FgbLaunch L) {
   const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
   if (p2 >= L.n[2]) return;
 #pragma unroll
