@@ -107,6 +107,7 @@ struct FgbProgramDesc {
   FgbAdjLaunchFn adj_gather[FGB_NUM_PRECISIONS][FGB_MAX_STAGES];
   int adj_pairs[FGB_MAX_STAGES];
   int adj_parts[FGB_MAX_STAGES];   // partial-sum kernels per stage
+  int adj_recompute[FGB_MAX_STAGES];   // forward arrays of the stage read by the partial sums
 };
 
 typedef const FgbProgramDesc* (*FgbProgramGetter)(void);

@@ -580,8 +580,10 @@ static int state_to_host(fgb_grid* g, const void* src, double* host) {
   return FGB_OK;
 }
 
-// Multi-stage step: recompute the step's forward arrays from u, then run the
-// two adjoint passes of each stage from the last stage to the first.
+// Multi-stage step: recompute from u the forward arrays that the partial
+// sums read (the generator works out which; a linear last stage needs none
+// of the arrays it reads), then run the adjoint passes of each stage from
+// the last stage to the first.
 static int stage_adjoint_step(fgb_grid* g, const void* u) {
   const FgbProgramDesc* d = g->prog;
   const size_t es = storage_size(g->precision), cs = compute_size(g->precision);
@@ -589,6 +591,7 @@ static int stage_adjoint_step(fgb_grid* g, const void* u) {
   fill_launch(g, g->cur, &L);
   for (int f = 0; f < d->nfields; ++f) L.in[f] = (const char*)u + f * g->cells * es;
   for (int st = 0; st + 1 < d->nstages; ++st) {
+    if (!d->adj_recompute[st]) continue;
     cudaError_t e = d->launch[g->precision][st](&L, g->stream);
     if (e != cudaSuccess) return cuda_fail(e, "stage launch");
     ++g->launches;

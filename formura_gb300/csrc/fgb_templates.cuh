@@ -519,7 +519,8 @@ struct AdjointStagePair {
   using P1 = Partial;
   using P2 = Gather;
 };
-template <class... Pairs>
+// Rec::kStage[s]: the adjoint step recomputes stage s's forward arrays
+template <class Rec, class... Pairs>
 struct AdjointStages {};
 // the partial-sum kernels of one stage, launched in order
 template <class... Parts>
@@ -544,8 +545,8 @@ struct StageAdjointFill {
   }
 };
 // FP64 (exact rounding) and FP32 forms; the others have no adjoint
-template <class Prog, class... Pairs>
-struct StageAdjointFill<Prog, AdjointStages<Pairs...>> {
+template <class Prog, class Rec, class... Pairs>
+struct StageAdjointFill<Prog, AdjointStages<Rec, Pairs...>> {
   static void fill(FgbProgramDesc& d) {
     static_assert(sizeof...(Pairs) == Prog::kStages, "one adjoint pair per stage");
     const int pairs[] = {Pairs::P1::kPairs...};
@@ -560,6 +561,7 @@ struct StageAdjointFill<Prog, AdjointStages<Pairs...>> {
     for (int s = 0; s < (int)sizeof...(Pairs); ++s) {
       d.adj_pairs[s] = pairs[s];
       d.adj_parts[s] = parts[s];
+      d.adj_recompute[s] = Rec::kStage[s] ? 1 : 0;
       d.adj_partial[0][s] = p0[s];
       d.adj_gather[0][s] = g0[s];
       d.adj_partial[2][s] = p2[s];

@@ -19,6 +19,7 @@ gradient of the runtime (``fgb_gradient_*``) calls this step.
 """
 from __future__ import annotations
 
+import re
 from typing import Dict, List, Tuple
 
 from .cuda import _ProgramEmitter, _StageEmitter, c_double
@@ -276,6 +277,37 @@ def _as_alg(h):
     return h
 
 
+_VAR = re.compile(r"\bt\d+\b")
+_LDM = re.compile(r"a\.template ldm<(\d+),")
+
+
+def _live_mids(lines: List[str]) -> set:
+    """Forward arrays whose values a partial-sum kernel really uses: the
+    ldm loads reachable from its stp lines through the SSA definitions (the
+    rest is dead code the compiler drops)."""
+    defs: Dict[str, str] = {}
+    roots: List[str] = []
+    for line in lines:
+        text = line.strip()
+        m = re.match(r"const \w+ (t\d+) = (.*);$", text)
+        if m:
+            defs[m.group(1)] = m.group(2)
+        elif text.startswith("a.template stp<"):
+            roots.append(text)
+    live: set = set()
+    todo = [v for r in roots for v in _VAR.findall(r)]
+    mids: set = set()
+    while todo:
+        v = todo.pop()
+        if v in live or v not in defs:
+            continue
+        live.add(v)
+        expr = defs[v]
+        mids.update(int(k) for k in _LDM.findall(expr))
+        todo.extend(_VAR.findall(expr))
+    return mids
+
+
 def _stage_outputs(st) -> List[tuple]:
     """The outputs of a stage in emission order: ('s', node) for a store of
     the new state, ('m', node) for a manifest array kept in HBM."""
@@ -324,6 +356,7 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
     shift3 = [pe.shift if i >= 3 - pe.dim else 0 for i in range(3)]
     pass1: Dict[int, str] = {}
     pair_lists: List[List[tuple]] = []
+    needed_mids: set = set()          # forward arrays the partial sums read
     for st in pe.stages:
         texts: List[str] = []
         outs = _stage_outputs(st)
@@ -365,6 +398,7 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
                     pairs.append(pair)
                 j = pairs.index(pair)
                 se.emit(f"a.template stp<{j}, {'true' if first else 'false'}>({alg.T(pair_val[pair])});")
+            needed_mids |= _live_mids(se.lines)
             body = "\n".join(se.lines)
             name = f"AdjStage{st.index}_{gi}"
             part_names.append(name)
@@ -404,9 +438,25 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
                              f"  template <class M, class A>\n"
                              f"  static __device__ __forceinline__ void run(const A& a, const typename M::U* __restrict__ U) {{\n"
                              f"    using T = typename M::T;\n    (void)U;\n" + "\n".join(lines) + "\n  }\n};\n")
+    # the stages an adjoint step recomputes: those whose arrays the partial
+    # sums read, and the stages those depend on
+    producer = {pe.mids.index(m): s.index for s in pe.stages for m in s.mid_out}
+    recompute = [False] * S
+    todo = sorted({producer[k] for k in needed_mids})
+    while todo:
+        s_ = todo.pop()
+        if recompute[s_]:
+            continue
+        recompute[s_] = True
+        for node in pe.stages[s_].nodes:
+            for mn in node.micro:
+                if mn.inst[0] == "loadcursor" and stage_of[mn.inst[2]] != s_:
+                    todo.append(stage_of[mn.inst[2]])
     src = "\n".join(pass1[s] + gathers[s] for s in range(S))
+    flags = ", ".join("true" if r else "false" for r in recompute)
+    src += f"struct AdjointRecompute {{\n  static constexpr bool kStage[{S}] = {{{flags}}};\n}};\n"
     pairs_list = ", ".join(f"fgb::AdjointStagePair<AdjStage{s}, AdjGather{s}>" for s in range(S))
-    src += f"using StageAdjointList = fgb::AdjointStages<{pairs_list}>;\n"
+    src += f"using StageAdjointList = fgb::AdjointStages<AdjointRecompute, {pairs_list}>;\n"
     return src, pair_lists
 
 

@@ -22,7 +22,7 @@
 #define __forceinline__ inline
 
 namespace fgb {
-template <class... Pairs>
+template <class Rec, class... Pairs>
 struct AdjointStages {};
 template <class Partial, class Gather>
 struct AdjointStagePair {
@@ -176,8 +176,17 @@ struct Runner {
     sweep<Gather, typename P::P2>(g);
     (void)most;
   }
-  template <class... Pairs, size_t... I>
-  static void reverse_pairs(Grid& g, fgb::AdjointStages<Pairs...>, std::index_sequence<I...>) {
+  template <class Rec, class... Pairs>
+  static void recompute_flags(Grid& g, fgb::AdjointStages<Rec, Pairs...>) {
+    recompute<Rec>(g);
+  }
+  template <class Rec>
+  static void recompute(Grid& g) {
+    int s = 0;
+    ((Rec::kStage[s++] ? sweep<FwdAcc, Stages>(g) : void()), ...);
+  }
+  template <class Rec, class... Pairs, size_t... I>
+  static void reverse_pairs(Grid& g, fgb::AdjointStages<Rec, Pairs...>, std::index_sequence<I...>) {
     using List = std::tuple<Pairs...>;
     int most = 0;
     constexpr size_t N = sizeof...(Pairs);
@@ -188,7 +197,7 @@ struct Runner {
       sweep<Adj1, typename Prog::Adjoint>(g);
       return 0;
     } else if constexpr (!std::is_same<typename Prog::StageAdjoint, void>::value) {
-      forward(g, Prog::kStages - 1);
+      recompute_flags(g, typename Prog::StageAdjoint{});
       g.lmids.assign((size_t)Prog::kMids * g.cells + 1, 0.0);
       reverse_pairs(g, typename Prog::StageAdjoint{}, std::make_index_sequence<Prog::kStages>{});
       return 0;
