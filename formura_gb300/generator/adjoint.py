@@ -115,6 +115,15 @@ class _Algebra:
     def div(self, a, b):
         return self.binop("/", a, b, "div")
 
+    def over(self, a, b):
+        """a / b for the derivative terms: through the reciprocal of b, which
+        is bound once per denominator (both partials of a quotient and every
+        later use share it), so a forward division costs one division in the
+        reverse sweep rather than two."""
+        if b[0] == "u":
+            return self.div(a, b)
+        return self.mul(a, self.fe.bind(f"M::div(T(1), {self.T(b)})"))
+
     def neg(self, a):
         if a[0] == "u":
             return ("u", _simplify(("neg", a[1])))
@@ -226,9 +235,9 @@ def emit_adjoint(mm: MMProgram, name: str, pe: _ProgramEmitter = None):
                         push(a, lambda: alg.mul(Y, value(b)))
                         push(b, lambda: alg.mul(Y, value(a)))
                     elif op == "/":
-                        push(a, lambda: alg.div(Y, value(b)))
+                        push(a, lambda: alg.over(Y, value(b)))
                         if not an.om_uniform(micro[b].key[1]):
-                            push(b, lambda: alg.neg(alg.div(alg.mul(Y, value(i)), value(b))))
+                            push(b, lambda: alg.neg(alg.over(alg.mul(Y, value(i)), value(b))))
                     elif op == "**":
                         A, B = alg.T(value(a)), alg.T(value(b))
                         push(a, lambda: alg.mul(Y, fe.bind(f"M::mul({B}, M::pow({A}, M::sub({B}, T(1))))")))
@@ -531,9 +540,9 @@ def _reverse_sweep(se, alg, an, fields, pe, stage_of, st, defs, order, bar, touc
                 push(a, lambda: alg.mul(Y, value(opk(b))))
                 push(b, lambda: alg.mul(Y, value(opk(a))))
             elif op == "/":
-                push(a, lambda: alg.div(Y, value(opk(b))))
+                push(a, lambda: alg.over(Y, value(opk(b))))
                 if not an.om_uniform(micro[b].key[1]) or micro[b].inst[0] in ("loadstatic", "loadcursor"):
-                    push(b, lambda: alg.neg(alg.div(alg.mul(Y, value(key)), value(opk(b)))))
+                    push(b, lambda: alg.neg(alg.over(alg.mul(Y, value(key)), value(opk(b)))))
             elif op == "**":
                 A, B = alg.T(value(opk(a))), alg.T(value(opk(b)))
                 push(a, lambda: alg.mul(Y, se.bind(f"M::mul({B}, M::pow({A}, M::sub({B}, T(1))))")))
