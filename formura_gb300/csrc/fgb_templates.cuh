@@ -16,11 +16,19 @@ namespace fgb {
 // ---------------------------------------------------------------------------
 // arithmetic policies
 // ---------------------------------------------------------------------------
+struct F64Fast;
+
 // FP64, rounding exactly like the reference's C: one IEEE rounding per SSA
 // operation, no contraction (the __d*_rn intrinsics are never fused).
 struct F64Exact {
   using T = double;
   using U = double;   // element type of the uniform table
+  // Arithmetic of the generated adjoints' derivative terms.  The adjoint
+  // recomputes the forward values with this policy, bit for bit, but sums
+  // its products of derivatives with contraction: a gradient is checked
+  // against finite differences and the dot-product test, not bit patterns,
+  // and a fused multiply-add is one FP64 instruction instead of two.
+  using Deriv = F64Fast;
   static __device__ __forceinline__ T add(T a, T b) { return __dadd_rn(a, b); }
   static __device__ __forceinline__ T sub(T a, T b) { return __dsub_rn(a, b); }
   static __device__ __forceinline__ T mul(T a, T b) { return __dmul_rn(a, b); }
@@ -98,6 +106,7 @@ struct F64Exact {
 struct F64Fast {
   using T = double;
   using U = double;
+  using Deriv = F64Fast;
   static __device__ __forceinline__ T add(T a, T b) { return a + b; }
   static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
@@ -127,6 +136,7 @@ struct F64Fast {
 struct F32 {
   using T = float;
   using U = float;
+  using Deriv = F32;
   static __device__ __forceinline__ T add(T a, T b) { return a + b; }
   static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }

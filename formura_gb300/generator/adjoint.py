@@ -100,8 +100,8 @@ class _Algebra:
                 if x == ("u", ("lit", 1.0)):
                     return y
         if k == "/" and b[0] == "u":
-            return self.fe.bind(f"M::mul({self.T(a)}, {self.T(('u', ('/', ('lit', 1.0), b[1])))})")
-        return self.fe.bind(f"M::{fn}({self.T(a)}, {self.T(b)})")
+            return self.fe.bind(f"D::mul({self.T(a)}, {self.T(('u', ('/', ('lit', 1.0), b[1])))})")
+        return self.fe.bind(f"D::{fn}({self.T(a)}, {self.T(b)})")
 
     def add(self, a, b):
         return self.binop("+", a, b, "add")
@@ -122,12 +122,12 @@ class _Algebra:
         reverse sweep rather than two."""
         if b[0] == "u":
             return self.div(a, b)
-        return self.mul(a, self.fe.bind(f"M::div(T(1), {self.T(b)})"))
+        return self.mul(a, self.fe.bind(f"D::div(T(1), {self.T(b)})"))
 
     def neg(self, a):
         if a[0] == "u":
             return ("u", _simplify(("neg", a[1])))
-        return self.fe.bind(f"M::neg({self.T(a)})")
+        return self.fe.bind(f"D::neg({self.T(a)})")
 
 
 def emit_adjoint(mm: MMProgram, name: str, pe: _ProgramEmitter = None):
@@ -215,8 +215,8 @@ def emit_adjoint(mm: MMProgram, name: str, pe: _ProgramEmitter = None):
                         fn = op[len("external-call/"):]
                         x = alg.T(value(a))
                         y = alg.T(value(i))
-                        d = {"sqrt": f"M::div(T(0.5), {y})", "exp": y, "log": f"M::div(T(1), {x})",
-                             "sin": f"M::cos({x})", "cos": f"M::neg(M::sin({x}))",
+                        d = {"sqrt": f"D::div(T(0.5), {y})", "exp": y, "log": f"D::div(T(1), {x})",
+                             "sin": f"D::cos({x})", "cos": f"D::neg(D::sin({x}))",
                              "fabs": f"({x} < T(0) ? T(-1) : T(1))"}.get(fn)
                         if d is None:
                             raise FormuraCompileError(f"no derivative for {fn}")
@@ -240,9 +240,9 @@ def emit_adjoint(mm: MMProgram, name: str, pe: _ProgramEmitter = None):
                             push(b, lambda: alg.neg(alg.over(alg.mul(Y, value(i)), value(b))))
                     elif op == "**":
                         A, B = alg.T(value(a)), alg.T(value(b))
-                        push(a, lambda: alg.mul(Y, fe.bind(f"M::mul({B}, M::pow({A}, M::sub({B}, T(1))))")))
+                        push(a, lambda: alg.mul(Y, fe.bind(f"D::mul({B}, D::pow({A}, D::sub({B}, T(1))))")))
                         if not an.om_uniform(micro[b].key[1]):
-                            push(b, lambda: alg.mul(Y, fe.bind(f"M::mul({alg.T(value(i))}, M::log({A}))")))
+                            push(b, lambda: alg.mul(Y, fe.bind(f"D::mul({alg.T(value(i))}, D::log({A}))")))
                     else:
                         raise FormuraCompileError(f"no derivative for {op}")
                 elif k == "triop":
@@ -265,13 +265,13 @@ def emit_adjoint(mm: MMProgram, name: str, pe: _ProgramEmitter = None):
         terms = acc[g]
         expr = terms[0] if terms else "T(0)"
         for t in terms[1:]:
-            expr = f"M::add({expr}, {t})"
+            expr = f"D::add({expr}, {t})"
         out.append(f"    a.template stl<{g}>({expr});")
     body = "\n".join("    " + l.strip() for l in lines) + "\n" + "\n".join(out)
     return (f"struct AdjointStep {{\n"
             f"  template <class M, class A>\n"
             f"  static __device__ __forceinline__ void run(const A& a, const typename M::U* __restrict__ U) {{\n"
-            f"    using T = typename M::T;\n    (void)U;\n{body}\n  }}\n}};\n"), pe
+            f"    using T = typename M::T;\n    using D = typename M::Deriv;\n    (void)U;\n{body}\n  }}\n}};\n"), pe
 
 
 # ---------------------------------------------------------------------------
@@ -414,7 +414,7 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
             texts.append(f"struct {name} {{\n"
                          f"  template <class M, class A>\n"
                          f"  static __device__ __forceinline__ void run(const A& a, const typename M::U* __restrict__ U) {{\n"
-                         f"    using T = typename M::T;\n    (void)U;\n{body}\n  }}\n}};\n")
+                         f"    using T = typename M::T;\n    using D = typename M::Deriv;\n    (void)U;\n{body}\n  }}\n}};\n")
         pair_lists.append(pairs)
         texts.append(f"struct AdjStage{st.index} {{\n"
                      f"  static constexpr int kPairs = {len(pairs)};\n"
@@ -520,8 +520,8 @@ def _reverse_sweep(se, alg, an, fields, pe, stage_of, st, defs, order, bar, touc
                 fn = op[len("external-call/"):]
                 x = alg.T(value(opk(a)))
                 y = alg.T(value(key))
-                d = {"sqrt": f"M::div(T(0.5), {y})", "exp": y, "log": f"M::div(T(1), {x})",
-                     "sin": f"M::cos({x})", "cos": f"M::neg(M::sin({x}))",
+                d = {"sqrt": f"D::div(T(0.5), {y})", "exp": y, "log": f"D::div(T(1), {x})",
+                     "sin": f"D::cos({x})", "cos": f"D::neg(D::sin({x}))",
                      "fabs": f"({x} < T(0) ? T(-1) : T(1))"}.get(fn)
                 if d is None:
                     raise FormuraCompileError(f"no derivative for {fn}")
@@ -545,9 +545,9 @@ def _reverse_sweep(se, alg, an, fields, pe, stage_of, st, defs, order, bar, touc
                     push(b, lambda: alg.neg(alg.over(alg.mul(Y, value(key)), value(opk(b)))))
             elif op == "**":
                 A, B = alg.T(value(opk(a))), alg.T(value(opk(b)))
-                push(a, lambda: alg.mul(Y, se.bind(f"M::mul({B}, M::pow({A}, M::sub({B}, T(1))))")))
+                push(a, lambda: alg.mul(Y, se.bind(f"D::mul({B}, D::pow({A}, D::sub({B}, T(1))))")))
                 if not an.om_uniform(micro[b].key[1]):
-                    push(b, lambda: alg.mul(Y, se.bind(f"M::mul({alg.T(value(key))}, M::log({A}))")))
+                    push(b, lambda: alg.mul(Y, se.bind(f"D::mul({alg.T(value(key))}, D::log({A}))")))
             else:
                 raise FormuraCompileError(f"no derivative for {op}")
         elif k == "triop":

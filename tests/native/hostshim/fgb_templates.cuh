@@ -38,6 +38,7 @@ namespace hostshim {
 struct Exact {
   using T = double;
   using U = double;
+  using Deriv = Exact;   // derivative terms: also one rounding per operation here
   static T add(T a, T b) { return a + b; }
   static T sub(T a, T b) { return a - b; }
   static T mul(T a, T b) { return a * b; }
