@@ -467,12 +467,12 @@ struct AdjPartialAccess {
   __device__ __forceinline__ T ldlm() const {
     return ro_load(static_cast<const T*>(L.lmid[K]) + lin(p0, p1, p2));
   }
-  // partial sum of pair J: stored by the first kernel of the stage that
-  // reaches it, added to by the others
-  template <int J, bool FIRST>
+  // partial sum J of this kernel: every partial-sum kernel of a stage owns
+  // its sums, so nothing here reads a sum back (the gather adds the kernels'
+  // sums of the same array and cursor)
+  template <int J>
   __device__ __forceinline__ void stp(T v) const {
-    T* a = static_cast<T*>(L.pair[J]) + lin(p0, p1, p2);
-    *a = FIRST ? v : v + *a;
+    static_cast<T*>(L.pair[J])[lin(p0, p1, p2)] = v;
   }
 };
 

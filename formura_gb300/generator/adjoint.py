@@ -347,9 +347,9 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
       sweep of its SSA chain with lam_o(p) for the outputs o of group g (lam
       of the new state is read at p + shift, where the forward wrote it) and
       adds, for every input read (x, c), lam_o(p) * do(p)/dx(p + c) to the
-      partial sum P_(x,c)(p); the first group that reaches a pair stores it.
-      Large stages are cut into groups of outputs so that no kernel spills;
-    * ``AdjGather<s>`` forms lam_x(q) = sum_c P_(x,c)(q - c) in a fixed order,
+      partial sum P_(x,c,g)(p) of its own.  Large stages are cut into groups
+      of outputs so that no kernel spills;
+    * ``AdjGather<s>`` forms lam_x(q) = sum_(c,g) P_(x,c,g)(q - c) in a fixed order,
       storing it for the first stage (in reverse order) that reads x and
       adding to it for the others.
 
@@ -373,7 +373,7 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
         ngroups = max(1, min(len(outs), -(-nmicro // _PARTIAL_MICRO_OPS)))
         per = -(-len(outs) // ngroups)
         groups = [outs[i:i + per] for i in range(0, len(outs), per)]
-        pairs: List[tuple] = []           # (x, c) pairs of the stage, in order of first touch
+        pairs: List[tuple] = []           # (x, c, group) partial sums of the stage, in kernel order
         part_names: List[str] = []
         for gi, group in enumerate(groups):
             se = _StageEmitter(pe, st)
@@ -402,11 +402,8 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
             pair_val: Dict[tuple, tuple] = {}
             _reverse_sweep(se, alg, an, fields, pe, stage_of, st, defs, order, bar, touched, pair_val)
             for pair in touched:
-                first = pair not in pairs
-                if first:
-                    pairs.append(pair)
-                j = pairs.index(pair)
-                se.emit(f"a.template stp<{j}, {'true' if first else 'false'}>({alg.T(pair_val[pair])});")
+                pairs.append(pair + (gi,))
+                se.emit(f"a.template stp<{len(pairs) - 1}>({alg.T(pair_val[pair])});")
             needed_mids |= _live_mids(se.lines)
             body = "\n".join(se.lines)
             name = f"AdjStage{st.index}_{gi}"

@@ -118,11 +118,8 @@ struct Partial {
   double ldl() const { return g->lnext[F * g->cells + g->lin(p0 + D0, p1 + D1, p2 + D2)]; }
   template <int K>
   double ldlm() const { return g->lmids[K * g->cells + g->lin(p0, p1, p2)]; }
-  template <int J, bool FIRST>
-  void stp(double v) const {
-    double& a = g->pairs[J * g->cells + g->lin(p0, p1, p2)];
-    a = FIRST ? v : v + a;
-  }
+  template <int J>
+  void stp(double v) const { g->pairs[J * g->cells + g->lin(p0, p1, p2)] = v; }
 };
 
 struct Gather {
