@@ -61,7 +61,8 @@ def test_reference_arm_line_on_a_small_grid(monkeypatch):
     monkeypatch.setenv("RANK", "0")
     from formura_gb300 import workloads as W
     spec = bench.workload_spec("gs2d")
-    spec.update(cfg=W.gs_config(64), shape=(64, 64))
+    # 64 + 2*1*4 = 72 = 2 blocks of 36 per axis
+    spec.update(cfg=W.gs_config(64), shape=(64, 64), cpu_tb=[(4, 36)])
 
     class Args:
         warmup, steps = 1, 3
@@ -73,3 +74,22 @@ def test_reference_arm_line_on_a_small_grid(monkeypatch):
     assert line["impl"] == "reference" and line["unit"] == "GLUP/s" and line["value"] > 0
     assert line["cpu_baseline"]["kind"] == "port"
     assert line["e2e"]["h2d_bytes_per_step"] == 0
+    assert sorted(line["config"]["probed_configs_GLUPs"]) == ["NoBlocking",
+                                                              "TemporalBlocking nt=4 grid_per_block=36"]
+    assert line["config"]["time_steps_per_bench_step"] in (1, 4)
+
+
+@pytest.mark.parametrize("name", ["gs2d", "heat3d", "hllc3d", "hlld3d"])
+def test_cpu_configs_of_the_workloads_are_valid(name):
+    """Every temporal-blocking candidate of the CPU legs satisfies the
+    reference's divisibility rule for its workload's grid and sleeve."""
+    from formura_gb300.generator.config import decode_config
+    from formura_gb300.generator.manifest import compile_program
+    from formura_gb300.host import builtin_program
+    spec = bench.workload_spec(name)
+    src, _ = builtin_program(spec["program"])
+    cfgs = bench.oracle_configs(spec)
+    assert len(cfgs) == 1 + len(spec["cpu_tb"]) >= 2
+    for label, _, cfg in cfgs:
+        blocking = compile_program(src, decode_config(cfg)).om.config.blocking
+        assert blocking.temporal == (label != "NoBlocking"), label
