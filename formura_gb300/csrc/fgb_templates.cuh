@@ -23,11 +23,13 @@ struct F64Fast;
 struct F64Exact {
   using T = double;
   using U = double;   // element type of the uniform table
-  // Arithmetic of the generated adjoints' derivative terms.  The adjoint
-  // recomputes the forward values with this policy, bit for bit, but sums
-  // its products of derivatives with contraction: a gradient is checked
-  // against finite differences and the dot-product test, not bit patterns,
-  // and a fused multiply-add is one FP64 instruction instead of two.
+  // Arithmetic of the generated adjoint kernels: contracted FP64.  The
+  // arrays an adjoint step recomputes for later stages keep this exact
+  // policy, but the forward values a partial-sum kernel differentiates and
+  // its derivative terms are contracted, and a quotient there is a product
+  // with the reciprocal that the derivative needs anyway.  A gradient is
+  // checked against finite differences and the dot-product identity, not bit
+  // patterns; a fused multiply-add is one FP64 instruction instead of two.
   using Deriv = F64Fast;
   static __device__ __forceinline__ T add(T a, T b) { return __dadd_rn(a, b); }
   static __device__ __forceinline__ T sub(T a, T b) { return __dsub_rn(a, b); }

@@ -55,7 +55,7 @@ class _OffsetEmitter(_StageEmitter):
     """Forward values of the step at cursor offset ``e`` from the thread's cell."""
 
     def __init__(self, prog, stage, shared_lines, memo, counter):
-        super().__init__(prog, stage)
+        super().__init__(prog, stage, policy="D", reciprocal=True)
         self.lines = shared_lines
         self.memo = memo
         self._counter = counter
@@ -376,9 +376,12 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
         pairs: List[tuple] = []           # (x, c, group) partial sums of the stage, in kernel order
         part_names: List[str] = []
         for gi, group in enumerate(groups):
-            se = _StageEmitter(pe, st)
+            # the forward at p in the derivative policy, quotients through the
+            # reciprocals the reverse sweep needs anyway; stores are no-ops and
+            # unused values are dropped
+            se = _StageEmitter(pe, st, policy="D", reciprocal=True)
             for node in st.nodes:
-                se.node(node)   # the forward at p; stores are no-ops, unused values are dropped
+                se.node(node)
             defs: Dict[tuple, tuple] = {}
             order: List[tuple] = []
             for node in st.nodes:

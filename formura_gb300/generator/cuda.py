@@ -331,9 +331,16 @@ def soft_cost_default() -> Optional[float]:
 
 
 class _StageEmitter:
-    def __init__(self, prog: "_ProgramEmitter", stage: Stage):
+    """Emits one stage's SSA chain.  ``policy`` names the arithmetic policy
+    of the operations (``M``, the kernel's, or ``D``, its derivative policy);
+    with ``reciprocal`` a quotient by a grid value is formed as a product
+    with the reciprocal, which then serves every later use of it."""
+
+    def __init__(self, prog: "_ProgramEmitter", stage: Stage, policy: str = "M", reciprocal: bool = False):
         self.p = prog
         self.stage = stage
+        self.P = policy
+        self.reciprocal = reciprocal
         self.lines: List[str] = []
         self.var: Dict[tuple, object] = {}     # key -> expression handle
         self.memo: Dict[tuple, tuple] = {}     # (expression, type) -> handle
@@ -367,7 +374,7 @@ class _StageEmitter:
         key = (h[1], self.as_T(h[2]))
         if key not in cache:
             name = self.fresh()
-            self.emit(f"const T {name} = M::mul(T({c_double(h[1])}), {key[1]});")
+            self.emit(f"const T {name} = {self.P}::mul(T({c_double(h[1])}), {key[1]});")
             cache[key] = name
         return cache[key]
 
@@ -432,11 +439,11 @@ class _StageEmitter:
             if op == "+":
                 return x
             if op == "-":
-                return self.bind(f"M::neg({self.as_T(x)})")
+                return self.bind(f"{self.P}::neg({self.as_T(x)})")
             f = op[len("external-call/"):]
             if f not in _EXT:
                 raise FormuraCompileError(f"external function {f} is not available on the GPU")
-            return self.bind(f"M::{_EXT[f]}({self.as_T(x)})")
+            return self.bind(f"{self.P}::{_EXT[f]}({self.as_T(x)})")
         if k == "binop":
             op = inst[1]
             a = self.operand(micro, inst[2])
@@ -451,32 +458,35 @@ class _StageEmitter:
                         if x[1] == 1.0:
                             return y
                         if x[1] == -1.0:
-                            return self.bind(f"M::neg({self.as_T(y)})")
+                            return self.bind(f"{self.P}::neg({self.as_T(y)})")
                         if is_pow2(x[1]) and y[0] != "scaled":
                             return ("scaled", x[1], y)
-                return self.bind(f"M::mul({self.as_T(a)}, {self.as_T(b)})")
+                return self.bind(f"{self.P}::mul({self.as_T(a)}, {self.as_T(b)})")
             if op in ("+", "-"):
                 if b[0] == "scaled":
                     c = b[1] if op == "+" else -b[1]
-                    return self.bind(f"M::fma(T({c_double(c)}), {self.as_T(b[2])}, {self.as_T(a)})")
+                    return self.bind(f"{self.P}::fma(T({c_double(c)}), {self.as_T(b[2])}, {self.as_T(a)})")
                 if a[0] == "scaled":
-                    rhs = self.as_T(b) if op == "+" else f"M::neg({self.as_T(b)})"
-                    return self.bind(f"M::fma(T({c_double(a[1])}), {self.as_T(a[2])}, {rhs})")
+                    rhs = self.as_T(b) if op == "+" else f"{self.P}::neg({self.as_T(b)})"
+                    return self.bind(f"{self.P}::fma(T({c_double(a[1])}), {self.as_T(a[2])}, {rhs})")
                 fn = "add" if op == "+" else "sub"
-                return self.bind(f"M::{fn}({self.as_T(a)}, {self.as_T(b)})")
+                return self.bind(f"{self.P}::{fn}({self.as_T(a)}, {self.as_T(b)})")
             if op == "/":
                 dep = micro[inst[3]].key[1]
                 if an.om_uniform(dep):
                     if b[0] == "lit" and is_pow2(b[1]):
-                        return self.bind(f"M::mul({self.as_T(a)}, T({c_double(1.0 / b[1])}))")
+                        return self.bind(f"{self.P}::mul({self.as_T(a)}, T({c_double(1.0 / b[1])}))")
                     rc = self.recip_handle(dep)
-                    return self.bind(f"M::divu({self.as_T(a)}, {self.as_T(b)}, {self.as_T(rc)})")
-                return self.bind(f"M::div({self.as_T(a)}, {self.as_T(b)})")
+                    return self.bind(f"{self.P}::divu({self.as_T(a)}, {self.as_T(b)}, {self.as_T(rc)})")
+                if self.reciprocal:
+                    r = self.bind(f"{self.P}::div(T(1), {self.as_T(b)})")
+                    return self.bind(f"{self.P}::mul({self.as_T(a)}, {self.as_T(r)})")
+                return self.bind(f"{self.P}::div({self.as_T(a)}, {self.as_T(b)})")
             if op == "**":
                 if b[0] == "lit" and b[1] == 2.0:
                     xa = self.as_T(a)
-                    return self.bind(f"M::mul({xa}, {xa})")
-                return self.bind(f"M::pow({self.as_T(a)}, {self.as_T(b)})")
+                    return self.bind(f"{self.P}::mul({xa}, {xa})")
+                return self.bind(f"{self.P}::pow({self.as_T(a)}, {self.as_T(b)})")
             raise FormuraCompileError(f"operator {op} is not supported by the GPU backend")
         if k == "triop":
             c = self.operand(micro, inst[2])
