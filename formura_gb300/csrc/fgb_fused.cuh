@@ -30,8 +30,6 @@ struct TileAccess {
   }
 };
 
-// Two horizontally adjacent points (lx even) for the packed FP32 form: an
-// even x offset is one aligned 8-byte load, an odd one two 4-byte loads.
 // Same tile, but stores go to registers: a thread computes several rows of
 // one column before writing any of them, so loads shared between the rows
 // (the vertical neighbours) are read from shared memory once.

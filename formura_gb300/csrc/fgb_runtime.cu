@@ -802,9 +802,11 @@ int fgb_attach(fgb_grid* g, const char* which, const double* uniforms, int nunif
     return fail(FGB_E_ARG, "%s does not match the step's state", name);
   if (nuniforms != d->nuniforms || (nuniforms > 0 && !uniforms))
     return fail(FGB_E_ARG, "%s needs %d uniform values, got %d", name, d->nuniforms, nuniforms);
-  for (int a = 0; a < 3; ++a) {
+  // every axis of the program (not only those longer than one point) must
+  // hold the attached function's reach and roll
+  for (int a = 3 - d->dim; a < 3; ++a) {
     const int need = d->reach > d->shift ? d->reach : d->shift;
-    if (g->n[a] > 1 && g->n[a] < need) return fail(FGB_E_ARG, "grid too small for %s", name);
+    if (g->n[a] < need) return fail(FGB_E_ARG, "grid too small for %s", name);
   }
   fgb_grid::Sub& s = g->sub[k];
   cudaFree(s.uniforms);

@@ -1,7 +1,8 @@
 """Temporal-blocking kernels (several steps per launch in shared-memory
 tiles): every variant gives the same state as one step per launch, bit for
 bit in FP64 and FP32, including grids that are not multiples of the tile and
-step counts that are not multiples of the fused depth."""
+step counts that are not multiples of the fused depth, and grids shorter
+than a tile's halo (every index wraps through the modulo path)."""
 import numpy as np
 import pytest
 
@@ -21,7 +22,7 @@ def _state(shape, seed):
     return np.stack([u, v])
 
 
-@pytest.mark.parametrize("shape", [(256, 256), (100, 70), (64, 200)])
+@pytest.mark.parametrize("shape", [(256, 256), (100, 70), (64, 200), (3, 5), (1, 9)])
 @pytest.mark.parametrize("prec", ["f64", "f32"])
 def test_every_variant_matches_single_steps(shape, prec):
     src, _ = builtin_program("gs2d")
@@ -76,7 +77,8 @@ def test_f16_fused_close_to_f32():
         assert W.rel_l2(fb[i], fa[i]) < 2e-2
 
 
-@pytest.mark.parametrize("shape", [(48, 48, 48), (40, 50, 70), (8, 40, 36), (96, 20, 130), (40, 72, 128)])
+@pytest.mark.parametrize("shape", [(48, 48, 48), (40, 50, 70), (8, 40, 36), (96, 20, 130), (40, 72, 128), (3, 5, 4),
+                                   (1, 2, 7)])
 @pytest.mark.parametrize("prec", ["f64", "f32"])
 def test_3d_streaming_variants_match_single_steps(shape, prec):
     """The 2.5D streaming kernels (K steps per launch, planes of the slowest
