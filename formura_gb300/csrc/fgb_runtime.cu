@@ -590,9 +590,14 @@ static int stage_adjoint_step(fgb_grid* g, const void* u) {
   FgbLaunch L;
   fill_launch(g, g->cur, &L);
   for (int f = 0; f < d->nfields; ++f) L.in[f] = (const char*)u + f * g->cells * es;
+  // The arrays recomputed here only feed the partial sums, which evaluate
+  // their own forward values in contracted arithmetic: in the FP64 form
+  // they are recomputed with the contracted FP64 kernels too (same storage,
+  // same uniform table).  The forward steps of a gradient stay exact.
+  const int rp = g->precision == FGB_F64 ? FGB_F64_FAST : g->precision;
   for (int st = 0; st + 1 < d->nstages; ++st) {
     if (!d->adj_recompute[st]) continue;
-    cudaError_t e = d->launch[g->precision][st](&L, g->stream);
+    cudaError_t e = d->launch[rp][st](&L, g->stream);
     if (e != cudaSuccess) return cuda_fail(e, "stage launch");
     ++g->launches;
   }
