@@ -505,6 +505,40 @@ struct AdjGatherAccess {
   }
 };
 
+// the partial-sum kernels of one stage, launched in order
+template <class... Parts>
+struct AdjParts {};
+
+// A partial-sum functor evaluated at its point for sum J alone: the other
+// sums are dropped, so only J's part of the functor survives compilation.
+template <class S, class T, int DIM, int SHIFT, int J>
+struct AdjCaptureAccess : AdjPartialAccess<S, T, DIM, SHIFT> {
+  T* out;
+  template <int J2>
+  __device__ __forceinline__ void stp(T v) const {
+    if constexpr (J2 == J) *out = v;
+  }
+};
+
+// Gather pass of a stage whose partial sums are its outputs' adjoints times
+// constants (a linear stage): instead of reading the stored sum J at q + D
+// it evaluates the stage's partial-sum functors there.
+template <class M, class S, class T, int DIM, int SHIFT, class Parts>
+struct AdjDirectAccess;
+template <class M, class S, class T, int DIM, int SHIFT, class... Parts>
+struct AdjDirectAccess<M, S, T, DIM, SHIFT, AdjParts<Parts...>> : AdjGatherAccess<S, T> {
+  template <int J, int D0, int D1, int D2>
+  __device__ __forceinline__ T ldp() const {
+    const FgbAdjLaunch& L = this->L;
+    T v = T(0);
+    const AdjCaptureAccess<S, T, DIM, SHIFT, J> c{
+        {L, wrap2<D0>(this->p0, L.n[0]), wrap2<D1>(this->p1, L.n[1]), wrap2<D2>(this->p2, L.n[2])}, &v};
+    const typename M::U* U = static_cast<const typename M::U*>(L.uniforms);
+    (Parts::template run<M>(c, U), ...);
+    return v;
+  }
+};
+
 template <class M, class Acc, class F>
 __global__ void __launch_bounds__(kBlockX) adj_stage_kernel(const __grid_constant__ FgbAdjLaunch L) {
   const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
@@ -526,6 +560,18 @@ cudaError_t launch_adj_stage(const FgbAdjLaunch* L, cudaStream_t stream) {
   return cudaGetLastError();
 }
 
+template <class Prog, int P, class Parts, class F>
+cudaError_t launch_adj_direct(const FgbAdjLaunch* L, cudaStream_t stream) {
+  using M = typename Precision<P>::M;
+  using S = typename Precision<P>::S;
+  using T = typename M::T;
+  using Acc = AdjDirectAccess<M, S, T, Prog::kDim, Prog::kShift, Parts>;
+  const int bx = L->n[2] >= kBlockX ? kBlockX : ((L->n[2] + 31) / 32) * 32;
+  dim3 grid((L->n[2] + bx - 1) / bx, L->n[1], L->n[0]);
+  adj_stage_kernel<M, Acc, F><<<grid, bx, 0, stream>>>(*L);
+  return cudaGetLastError();
+}
+
 template <class Partial, class Gather>
 struct AdjointStagePair {
   using P1 = Partial;
@@ -534,9 +580,6 @@ struct AdjointStagePair {
 // Rec::kStage[s]: the adjoint step recomputes stage s's forward arrays
 template <class Rec, class... Pairs>
 struct AdjointStages {};
-// the partial-sum kernels of one stage, launched in order
-template <class... Parts>
-struct AdjParts {};
 template <class Prog, int P, class List>
 struct PartialLauncher;
 template <class Prog, int P, class... Parts>
@@ -546,6 +589,23 @@ struct PartialLauncher<Prog, P, AdjParts<Parts...>> {
     cudaError_t e = cudaSuccess;
     ((e = (e == cudaSuccess ? launch_adj_stage<Prog, P, Parts, false>(L, stream) : e)), ...);
     return e;
+  }
+};
+// the two passes of one stage's adjoint: partial sums and gather, or for a
+// linear stage the gather alone, forming its partial sums itself
+template <class Prog, int P, class Pair>
+struct StagePassLaunchers {
+  using P1 = typename Pair::P1;
+  static constexpr bool kDirect = P1::kDirect;
+  static constexpr int kPartials = kDirect ? 0 : PartialLauncher<Prog, P, typename P1::Parts>::kCount;
+  static cudaError_t none(const FgbAdjLaunch*, cudaStream_t) { return cudaSuccess; }
+  static FgbAdjLaunchFn partial() {
+    if constexpr (kDirect) return &none;
+    else return &PartialLauncher<Prog, P, typename P1::Parts>::launch;
+  }
+  static FgbAdjLaunchFn gather() {
+    if constexpr (kDirect) return &launch_adj_direct<Prog, P, typename P1::Parts, typename Pair::P2>;
+    else return &launch_adj_stage<Prog, P, typename Pair::P2, true>;
   }
 };
 
@@ -561,12 +621,12 @@ template <class Prog, class Rec, class... Pairs>
 struct StageAdjointFill<Prog, AdjointStages<Rec, Pairs...>> {
   static void fill(FgbProgramDesc& d) {
     static_assert(sizeof...(Pairs) == Prog::kStages, "one adjoint pair per stage");
-    const int pairs[] = {Pairs::P1::kPairs...};
-    const int parts[] = {PartialLauncher<Prog, 0, typename Pairs::P1::Parts>::kCount...};
-    const FgbAdjLaunchFn p0[] = {&PartialLauncher<Prog, 0, typename Pairs::P1::Parts>::launch...};
-    const FgbAdjLaunchFn g0[] = {&launch_adj_stage<Prog, 0, typename Pairs::P2, true>...};
-    const FgbAdjLaunchFn p2[] = {&PartialLauncher<Prog, 2, typename Pairs::P1::Parts>::launch...};
-    const FgbAdjLaunchFn g2[] = {&launch_adj_stage<Prog, 2, typename Pairs::P2, true>...};
+    const int pairs[] = {(Pairs::P1::kDirect ? 0 : Pairs::P1::kPairs)...};
+    const int parts[] = {StagePassLaunchers<Prog, 0, Pairs>::kPartials...};
+    const FgbAdjLaunchFn p0[] = {StagePassLaunchers<Prog, 0, Pairs>::partial()...};
+    const FgbAdjLaunchFn g0[] = {StagePassLaunchers<Prog, 0, Pairs>::gather()...};
+    const FgbAdjLaunchFn p2[] = {StagePassLaunchers<Prog, 2, Pairs>::partial()...};
+    const FgbAdjLaunchFn g2[] = {StagePassLaunchers<Prog, 2, Pairs>::gather()...};
     for (int p = 0; p < FGB_NUM_PRECISIONS; ++p)
       for (int s = 0; s < FGB_MAX_STAGES; ++s) d.adj_partial[p][s] = d.adj_gather[p][s] = nullptr;
     static_assert(((Pairs::P1::kPairs <= FGB_MAX_PAIRS) && ...), "too many (array, cursor) pairs in a stage");

@@ -329,6 +329,43 @@ def _stage_outputs(st) -> List[tuple]:
     return out
 
 
+def _stage_is_linear(an, st) -> bool:
+    """True when every output of the stage is a linear combination of its
+    inputs with grid-independent coefficients: no product or quotient of two
+    grid values, no function, power, comparison or selection on one.  The
+    partial sums of such a stage are the adjoints of its outputs times
+    constants, so they are cheaper to form where they are gathered than to
+    store."""
+    for node in st.nodes:
+        micro = node.micro
+        for mn in micro:
+            inst = mn.inst
+            k = inst[0]
+            if k in ("imm", "loadstatic", "loadcursor", "loadindex", "store") or an.om_uniform(mn.key[1]):
+                continue
+
+            def grid(j):
+                return not an.om_uniform(micro[j].key[1]) or micro[j].inst[0] in ("loadstatic", "loadcursor")
+
+            if k == "uniop":
+                if inst[1] not in ("+", "-"):
+                    return False
+            elif k == "binop":
+                op, a, b = inst[1], inst[2], inst[3]
+                if op in _CMP or op == "**":
+                    return False
+                if op == "*" and grid(a) and grid(b):
+                    return False
+                if op == "/" and grid(b):
+                    return False
+            elif k == "triop":
+                if grid(inst[2]):
+                    return False
+            else:
+                return False
+    return True
+
+
 # a partial-sum kernel holds the forward values of its outputs' backward
 # slice in registers: stages larger than this many micro operations are cut
 # into several kernels by output, so that none of them spills
@@ -351,7 +388,11 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
       of outputs so that no kernel spills;
     * ``AdjGather<s>`` forms lam_x(q) = sum_(c,g) P_(x,c,g)(q - c) in a fixed order,
       storing it for the first stage (in reverse order) that reads x and
-      adding to it for the others.
+      adding to it for the others;
+    * a stage whose outputs are linear in its inputs with grid-independent
+      coefficients (``kDirect``) launches no partial-sum kernel: its gather
+      evaluates the partial-sum functors at q - c itself, which reads the
+      adjoints of the outputs instead of the (more numerous) stored sums.
 
     Stages run from last to first, after the forward arrays of the step were
     recomputed from u_n.  Nothing is atomic, so the result is deterministic.
@@ -416,8 +457,10 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
                          f"  static __device__ __forceinline__ void run(const A& a, const typename M::U* __restrict__ U) {{\n"
                          f"    using T = typename M::T;\n    using D = typename M::Deriv;\n    (void)U;\n{body}\n  }}\n}};\n")
         pair_lists.append(pairs)
+        direct = "true" if _stage_is_linear(an, st) else "false"
         texts.append(f"struct AdjStage{st.index} {{\n"
                      f"  static constexpr int kPairs = {len(pairs)};\n"
+                     f"  static constexpr bool kDirect = {direct};\n"
                      f"  using Parts = fgb::AdjParts<{', '.join(part_names)}>;\n}};\n")
         pass1[st.index] = "\n".join(texts)
     # gathers, in the order the adjoint runs them (last stage first)

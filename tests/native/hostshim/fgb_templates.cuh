@@ -139,6 +139,30 @@ struct Gather {
   }
 };
 
+// sum J of a partial-sum functor at its point; the others are dropped
+template <int J>
+struct Capture : Partial {
+  double* out;
+  template <int J2>
+  void stp(double v) const {
+    if (J2 == J) *out = v;
+  }
+};
+
+// gather of a linear stage: the partial sums are formed where they are read
+template <class Parts>
+struct Direct;
+template <class... Parts>
+struct Direct<fgb::AdjParts<Parts...>> : Gather {
+  template <int J, int D0, int D1, int D2>
+  double ldp() const {
+    double v = 0.0;
+    const Capture<J> c{{g, p0 + D0, p1 + D1, p2 + D2}, &v};
+    (Parts::template run<Exact>(c, g->U), ...);
+    return v;
+  }
+};
+
 template <class Acc, class F>
 void sweep(Grid& g) {
   for (int i = 0; i < g.n[0]; ++i)
@@ -169,9 +193,13 @@ struct Runner {
   }
   template <class P>
   static void stage_pair(Grid& g, int& most) {
-    g.pairs.assign((size_t)P::P1::kPairs * g.cells + 1, 0.0);
-    partials(g, typename P::P1::Parts{});
-    sweep<Gather, typename P::P2>(g);
+    if constexpr (P::P1::kDirect) {
+      sweep<Direct<typename P::P1::Parts>, typename P::P2>(g);
+    } else {
+      g.pairs.assign((size_t)P::P1::kPairs * g.cells + 1, 0.0);
+      partials(g, typename P::P1::Parts{});
+      sweep<Gather, typename P::P2>(g);
+    }
     (void)most;
   }
   template <class Rec, class... Pairs>
