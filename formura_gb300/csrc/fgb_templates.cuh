@@ -592,11 +592,16 @@ struct PartialLauncher<Prog, P, AdjParts<Parts...>> {
   }
 };
 // the two passes of one stage's adjoint: partial sums and gather, or for a
-// linear stage the gather alone, forming its partial sums itself
+// linear stage the gather alone, forming its partial sums itself.  Only the
+// FP32 forms do the latter: there the stage's adjoint is bound by HBM and
+// the direct gather moves a quarter of the bytes (HLLC's update stage:
+// 0.94 -> 0.32 ms at 256^3), while the FP64 form is bound by the FP64 pipe
+// and forming the sums once per cursor costs more than storing them
+// (2.17 -> 2.41 ms).
 template <class Prog, int P, class Pair>
 struct StagePassLaunchers {
   using P1 = typename Pair::P1;
-  static constexpr bool kDirect = P1::kDirect;
+  static constexpr bool kDirect = P1::kDirect && std::is_same<typename Precision<P>::M::T, float>::value;
   static constexpr int kPartials = kDirect ? 0 : PartialLauncher<Prog, P, typename P1::Parts>::kCount;
   static cudaError_t none(const FgbAdjLaunch*, cudaStream_t) { return cudaSuccess; }
   static FgbAdjLaunchFn partial() {
@@ -621,7 +626,7 @@ template <class Prog, class Rec, class... Pairs>
 struct StageAdjointFill<Prog, AdjointStages<Rec, Pairs...>> {
   static void fill(FgbProgramDesc& d) {
     static_assert(sizeof...(Pairs) == Prog::kStages, "one adjoint pair per stage");
-    const int pairs[] = {(Pairs::P1::kDirect ? 0 : Pairs::P1::kPairs)...};
+    const int pairs[] = {Pairs::P1::kPairs...};
     const int parts[] = {StagePassLaunchers<Prog, 0, Pairs>::kPartials...};
     const FgbAdjLaunchFn p0[] = {StagePassLaunchers<Prog, 0, Pairs>::partial()...};
     const FgbAdjLaunchFn g0[] = {StagePassLaunchers<Prog, 0, Pairs>::gather()...};
