@@ -35,20 +35,53 @@ struct F64Exact {
   static __device__ __forceinline__ T sub(T a, T b) { return __dsub_rn(a, b); }
   static __device__ __forceinline__ T mul(T a, T b) { return __dmul_rn(a, b); }
   static __device__ __forceinline__ T div(T a, T b) { return __ddiv_rn(a, b); }
-  // a*b + c where a*b is exact (a is a power of two): same result as the
-  // separately rounded product and sum.
-  static __device__ __forceinline__ T fma(T a, T b, T c) { return __fma_rn(a, b, c); }
-  // x / c for a grid-independent c with rc = RN(1/c): Markstein's
-  // correction step gives the correctly rounded quotient.
+
+  // The shortened forms below equal the reference's separately rounded
+  // operations only while no intermediate leaves the normal range.  Each
+  // checks its operands' exponents on the integer pipe and takes a
+  // warp-uniform branch: a lane whose operands fall outside sends its warp
+  // to the plain IEEE instructions, so no lane issues both forms.
+  static __device__ __forceinline__ uint64_t bits(T x) { return (uint64_t)__double_as_longlong(x); }
+  static __device__ __forceinline__ unsigned expo(T x) { return (unsigned)(bits(x) >> 52) & 0x7ffu; }
+  static __device__ __forceinline__ bool is_zero(T x) { return (bits(x) << 1) == 0; }
+  static __device__ __forceinline__ bool warp_all(bool ok) { return __all_sync(__activemask(), ok); }
+  // biased exponent field within [1023 - w, 1023 + w]
+  static __device__ __forceinline__ bool within(T x, unsigned w) { return expo(x) - (1023u - w) <= 2u * w; }
+
+  // a*h + t for a = +-2^k (a literal): one rounding of the exact sum, which
+  // is the reference's RN(RN(a*h) + t) as long as a*h is exact, that is h
+  // is zero or a*h stays normal.
+  static __device__ __forceinline__ T fma(T a, T h, T t) {
+    const int k = (int)expo(a) - 1023;
+    const bool ok = is_zero(h) || (unsigned)((int)expo(h) + k - 1) <= 2045u;
+    if (warp_all(ok)) return __fma_rn(a, h, t);
+    return __dadd_rn(__dmul_rn(a, h), t);
+  }
+  // q = RN(x / c) from y = RN(1 / c): Markstein's correction of RN(x * y),
+  // exact when x - q*c is representable and q normal.  Zero numerators take
+  // RN(x * y) itself, which carries the quotient's sign.
+  static __device__ __forceinline__ T markstein(T x, T c, T y) {
+    const T q = __dmul_rn(x, y);
+    const T e = __fma_rn(-q, c, x);
+    return is_zero(x) ? q : __fma_rn(e, y, q);
+  }
+  // x / c for a grid-independent c with rc = RN(1/c) from the host:
+  // numerators in [2^-900, 2^900] or zero, c in [2^-100, 2^100].
   static __device__ __forceinline__ T divu(T x, T c, T rc) {
 #ifdef FGB_DIVU_IEEE
     (void)rc;
     return __ddiv_rn(x, c);
 #else
-    const T q = __dmul_rn(x, rc);
-    const T e = __fma_rn(-q, c, x);
-    return __fma_rn(e, rc, q);
+    if (warp_all(within(c, 100) && (is_zero(x) || within(x, 900)))) return markstein(x, c, rc);
+    return __ddiv_rn(x, c);
 #endif
+  }
+  // RN(1/b) for a grid value b that several quotients divide by
+  static __device__ __forceinline__ T rcp(T b) { return __drcp_rn(b); }
+  // a / b with y = rcp(b): operands in [2^-400, 2^400] (a may be zero)
+  static __device__ __forceinline__ T divr(T a, T b, T y) {
+    if (warp_all(within(b, 400) && (is_zero(a) || within(a, 400)))) return markstein(a, b, y);
+    return __ddiv_rn(a, b);
   }
   // The same operations on the integer pipes (fgb_softf64.h), with the
   // hardware instruction for the operands outside the fast path: the
@@ -81,7 +114,7 @@ struct F64Exact {
     uint64_t r;
     const bool ok = soft::scaled_add_bits(soft::to_bits(c), soft::to_bits(h), soft::to_bits(t), r);
     T v = soft::from_bits(r);
-    if (__any_sync(__activemask(), !ok)) v = ok ? v : __fma_rn(c, h, t);
+    if (__any_sync(__activemask(), !ok)) v = ok ? v : fma(c, h, t);
     return v;
   }
   // Markstein quotient with its first product on the integer pipes
@@ -90,9 +123,10 @@ struct F64Exact {
     (void)rc;
     return __ddiv_rn(x, c);
 #endif
+    if (!warp_all(within(c, 100) && (is_zero(x) || within(x, 900)))) return __ddiv_rn(x, c);
     const T q = smul(x, rc);
     const T e = __fma_rn(-q, c, x);
-    return __fma_rn(e, rc, q);
+    return is_zero(x) ? q : __fma_rn(e, rc, q);
   }
   static __device__ __forceinline__ T neg(T a) { return -a; }
   static __device__ __forceinline__ T sqrt(T a) { return __dsqrt_rn(a); }
@@ -115,6 +149,8 @@ struct F64Fast {
   static __device__ __forceinline__ T div(T a, T b) { return a / b; }
   static __device__ __forceinline__ T fma(T a, T b, T c) { return ::fma(a, b, c); }
   static __device__ __forceinline__ T divu(T x, T, T rc) { return x * rc; }
+  static __device__ __forceinline__ T rcp(T b) { return __drcp_rn(b); }
+  static __device__ __forceinline__ T divr(T a, T, T y) { return a * y; }
   static __device__ __forceinline__ T sadd(T a, T b) { return a + b; }
   static __device__ __forceinline__ T ssub(T a, T b) { return a - b; }
   static __device__ __forceinline__ T smul(T a, T b) { return a * b; }
@@ -147,6 +183,8 @@ struct F32 {
   static __device__ __forceinline__ T div(T a, T b) { return __fdividef(a, b); }
   static __device__ __forceinline__ T fma(T a, T b, T c) { return fmaf(a, b, c); }
   static __device__ __forceinline__ T divu(T x, T, T rc) { return x * rc; }
+  static __device__ __forceinline__ T rcp(T b) { return __fdividef(1.0f, b); }
+  static __device__ __forceinline__ T divr(T a, T, T y) { return a * y; }
   static __device__ __forceinline__ T sadd(T a, T b) { return a + b; }
   static __device__ __forceinline__ T ssub(T a, T b) { return a - b; }
   static __device__ __forceinline__ T smul(T a, T b) { return a * b; }

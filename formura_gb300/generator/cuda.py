@@ -336,11 +336,18 @@ class _StageEmitter:
     with ``reciprocal`` a quotient by a grid value is formed as a product
     with the reciprocal, which then serves every later use of it."""
 
-    def __init__(self, prog: "_ProgramEmitter", stage: Stage, policy: str = "M", reciprocal: bool = False):
+    def __init__(self, prog: "_ProgramEmitter", stage: Stage, policy: str = "M", reciprocal: bool = False,
+                 div_uses: Optional[Dict[str, int]] = None):
         self.p = prog
         self.stage = stage
         self.P = policy
         self.reciprocal = reciprocal
+        # quotients per grid denominator, from an earlier pass over the same
+        # stage: a denominator with several gets one reciprocal (M::rcp) and
+        # its quotients M::divr
+        self.div_uses = div_uses or {}
+        self.div_seen: Dict[str, int] = {}
+        self.nr = 0
         self.lines: List[str] = []
         self.var: Dict[tuple, object] = {}     # key -> expression handle
         self.memo: Dict[tuple, tuple] = {}     # (expression, type) -> handle
@@ -481,7 +488,12 @@ class _StageEmitter:
                 if self.reciprocal:
                     r = self.bind(f"{self.P}::div(T(1), {self.as_T(b)})")
                     return self.bind(f"{self.P}::mul({self.as_T(a)}, {self.as_T(r)})")
-                return self.bind(f"{self.P}::div({self.as_T(a)}, {self.as_T(b)})")
+                den = self.as_T(b)
+                self.div_seen[den] = self.div_seen.get(den, 0) + 1
+                if self.div_uses.get(den, 0) >= 2:
+                    y = self.bind(f"{self.P}::rcp({den})", prefix="r")
+                    return self.bind(f"{self.P}::divr({self.as_T(a)}, {den}, {self.as_T(y)})")
+                return self.bind(f"{self.P}::div({self.as_T(a)}, {den})")
             if op == "**":
                 if b[0] == "lit" and b[1] == 2.0:
                     xa = self.as_T(a)
@@ -522,13 +534,19 @@ class _StageEmitter:
             return expr
         return expr
 
-    def bind(self, expr: str, ctype: str = "T"):
+    def bind(self, expr: str, ctype: str = "T", prefix: Optional[str] = None):
         # value numbering: the same operation on the same operands is the same
-        # value (every operation is deterministic), so it is computed once
+        # value (every operation is deterministic), so it is computed once.
+        # Reciprocals are named apart so that the other names do not depend
+        # on whether a pass shares denominators.
         hit = self.memo.get((expr, ctype))
         if hit is not None:
             return hit
-        name = self.fresh()
+        if prefix is None:
+            name = self.fresh()
+        else:
+            self.nr += 1
+            name = f"{prefix}{self.nr}"
         self.emit(f"const {ctype} {name} = {self.pipe(expr)};")
         h = ("v", name, ctype)
         self.memo[(expr, ctype)] = h
@@ -592,7 +610,10 @@ class _ProgramEmitter:
                f"namespace fgb_gen_{self.name} {{", ""]
         stage_texts = []
         for st in self.stages:
-            se = _StageEmitter(self, st)
+            count = _StageEmitter(self, st)      # a pass that counts quotients per denominator
+            for node in st.nodes:
+                count.node(node)
+            se = _StageEmitter(self, st, div_uses=count.div_seen)
             for node in st.nodes:
                 se.node(node)
             body = "\n".join(se.lines)

@@ -1,0 +1,79 @@
+// GPU check of the shortened operations of the bit-faithful FP64 policy
+// (fgb::F64Exact::divu, ::divr with ::rcp, ::fma with a power-of-two factor)
+// against the reference's separately rounded IEEE operations, bit for bit.
+// Operand classes are chosen per warp, so that warps whose lanes all lie in
+// the shortened forms' range take them, and others (subnormal, tiny, huge,
+// infinite or NaN operands, signed zeros) take the fallback, alone or mixed.
+#include <cuda_runtime.h>
+#include <stdint.h>
+#include "../../formura_gb300/csrc/fgb_templates.cuh"
+
+using fgb::F64Exact;
+
+__device__ __forceinline__ uint64_t mix(uint64_t x) {
+  // splitmix64 finaliser
+  x += 0x9e3779b97f4a7c15ull;
+  x = (x ^ (x >> 30)) * 0xbf58476d1ce4e5b9ull;
+  x = (x ^ (x >> 27)) * 0x94d049bb133111ebull;
+  return x ^ (x >> 31);
+}
+
+__device__ __forceinline__ double make(uint64_t sign, int e, uint64_t mant) {
+  e = e < 0 ? 0 : (e > 2047 ? 2047 : e);
+  return __longlong_as_double((long long)((sign << 63) | ((uint64_t)e << 52) | (mant & 0x000fffffffffffffull)));
+}
+
+// one operand of class `cls` (the same for the whole warp)
+__device__ double operand(uint64_t key, int cls) {
+  const uint64_t r = mix(key), m = mix(key ^ 0xabcdef);
+  const uint64_t sign = r >> 63;
+  switch (cls) {
+    case 0:  return make(sign, 1023 - 60 + (int)(r % 121), m);          // moderate
+    case 1:  return make(sign, 1023 - 380 + (int)(r % 761), m);         // wide, inside the windows
+    case 2:  return make(sign, (int)(r % 90), m >> (r % 53));           // subnormal and lowest binades
+    case 3:  return make(sign, 1960 + (int)(r % 88), m);                // huge, infinity and NaN
+    case 4:  return (r & 2) ? make(sign, 0, 0) : make(sign, 1023 - 60 + (int)(r % 121), m);  // signed zeros
+    default: return __longlong_as_double((long long)r);                 // any bit pattern
+  }
+}
+
+__device__ __forceinline__ bool same(double a, double b) {
+  // bitwise, except that any NaN matches any NaN
+  return __double_as_longlong(a) == __double_as_longlong(b) || (a != a && b != b);
+}
+
+__global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
+  unsigned long long bad[3] = {0, 0, 0};
+  const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
+  for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
+    const uint64_t key = seed * 0x100000000ull + i;
+    const uint64_t warp = i / 32;
+    const int ca = (int)(mix(warp * 3 + seed) % 6), cb = (int)(mix(warp * 5 + seed) % 6);
+    // divu: uniform divisor per warp (grid-independent), numerator per lane
+    const double c = operand(warp * 11 + seed, ca == 3 ? 1 : ca % 2);
+    const double rc = 1.0 / c;
+    const double x = operand(key * 7 + 1, cb == 5 ? (int)(mix(key) % 6) : cb);
+    if (!same(F64Exact::divu(x, c, rc), __ddiv_rn(x, c))) ++bad[0];
+    // divr: grid numerator and denominator
+    const double a = operand(key * 7 + 2, ca == 5 ? (int)(mix(key ^ 1) % 6) : ca);
+    const double b = operand(key * 7 + 3, cb);
+    if (!same(F64Exact::divr(a, b, F64Exact::rcp(b)), __ddiv_rn(a, b))) ++bad[1];
+    // fma with a = +-2^k, k in [-3, 3]: RN(RN(a*h) + t)
+    const int k = (int)(mix(warp * 7 + seed) % 7) - 3;
+    const double f = ((warp & 1) ? -1.0 : 1.0) * ldexp(1.0, k);
+    const double h = operand(key * 7 + 4, cb), t = operand(key * 7 + 5, (cb + 1) % 6);
+    if (!same(F64Exact::fma(f, h, t), __dadd_rn(__dmul_rn(f, h), t))) ++bad[2];
+  }
+  for (int j = 0; j < 3; ++j) atomicAdd(&out[j], bad[j]);
+}
+
+extern "C" int exact_forms_gpu_check(unsigned long long seed, unsigned long long n, unsigned long long* host_out) {
+  unsigned long long* d = nullptr;
+  if (cudaMalloc(&d, 3 * sizeof(unsigned long long)) != cudaSuccess) return 1;
+  cudaMemset(d, 0, 3 * sizeof(unsigned long long));
+  check<<<152 * 8, 256>>>(seed, n, d);
+  cudaError_t e = cudaDeviceSynchronize();
+  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  cudaFree(d);
+  return e == cudaSuccess ? 0 : 2;
+}

@@ -45,6 +45,8 @@ struct Exact {
   static T div(T a, T b) { return a / b; }
   static T fma(T a, T b, T c) { return std::fma(a, b, c); }   // a is a power of two: exact product
   static T divu(T x, T c, T) { return x / c; }                // the device's corrected quotient is this
+  static T rcp(T b) { return 1.0 / b; }
+  static T divr(T a, T b, T) { return a / b; }                // likewise
   static T sadd(T a, T b) { return a + b; }
   static T ssub(T a, T b) { return a - b; }
   static T smul(T a, T b) { return a * b; }

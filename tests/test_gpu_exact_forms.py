@@ -1,0 +1,34 @@
+"""The shortened operations of the bit-faithful FP64 policy on the GPU
+(division by a grid-independent constant through its host reciprocal, a
+quotient through a shared reciprocal, a multiply-add by a power of two)
+against the reference's separately rounded IEEE operations: bit for bit on
+2^28 operands per seed, including subnormal, tiny, huge and non-finite
+operands and signed zeros, where they fall back to the IEEE instructions."""
+import ctypes
+import os
+import subprocess
+
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+ROOT = os.path.dirname(HERE)
+
+
+@pytest.fixture(scope="module")
+def lib(tmp_path_factory):
+    out = str(tmp_path_factory.mktemp("exactgpu") / "libexactgpu.so")
+    subprocess.check_call(["nvcc", "-gencode", "arch=compute_103a,code=sm_103a", "-O3", "-std=c++17",
+                           "-Xcompiler", "-fPIC", "-shared", os.path.join(HERE, "native", "exact_forms_gpu.cu"),
+                           "-o", out])
+    L = ctypes.CDLL(out)
+    L.exact_forms_gpu_check.argtypes = [ctypes.c_ulonglong, ctypes.c_ulonglong, ctypes.POINTER(ctypes.c_ulonglong)]
+    return L
+
+
+@pytest.mark.parametrize("seed", [1, 2, 3])
+def test_exact_forms_match_ieee(lib, seed):
+    out = (ctypes.c_ulonglong * 3)()
+    assert lib.exact_forms_gpu_check(seed, 2**28, out) == 0
+    assert list(out) == [0, 0, 0], ("divu, divr, fma mismatches", list(out))

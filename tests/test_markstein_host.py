@@ -1,0 +1,18 @@
+"""The operand windows of the bit-faithful FP64 policy's division through a
+reciprocal (Markstein's correction of RN(a * RN(1/b))), checked on the host
+with its correctly rounded fma: bit-identical to RN(a/b) on 2 * 10^7 operand
+pairs inside the windows, including signed zero numerators; not so for
+subnormal numerators, which therefore take the IEEE division on the device."""
+import os
+import subprocess
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+
+
+def test_markstein_windows(tmp_path):
+    exe = str(tmp_path / "markstein_host")
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", os.path.join(HERE, "native", "markstein_host.c"),
+                           "-o", exe, "-lm"])
+    inside, outside = map(int, subprocess.check_output([exe, "10000000"], text=True).split())
+    assert inside == 0
+    assert outside > 0
