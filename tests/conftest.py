@@ -10,3 +10,10 @@ REFERENCE = "/root/reference"
 
 def pytest_configure(config):
     config.addinivalue_line("markers", "gpu: needs a GB300 GPU and the CUDA library")
+
+
+def bits_equal(a, b) -> bool:
+    """Bit-for-bit equality of two arrays (so +0 and -0 differ, unlike ==)."""
+    import numpy as np
+    a, b = np.ascontiguousarray(a), np.ascontiguousarray(b)
+    return a.shape == b.shape and a.dtype == b.dtype and a.tobytes() == b.tobytes()

@@ -6,6 +6,7 @@ import pytest
 
 from formura_gb300 import workloads as W
 from formura_gb300.host import Batch, Grid, builtin_program, program_uniforms
+from conftest import bits_equal
 
 pytestmark = pytest.mark.gpu
 
@@ -38,7 +39,7 @@ def test_batch_matches_single_grids(prec):
         b.set_variant(v["index"])
         b.forward(steps)
         for i in range(len(members)):
-            assert np.array_equal(b.download(i), ref[i]), (v, i)
+            assert bits_equal(b.download(i), ref[i]), (v, i)
     b.close()
 
 
@@ -51,5 +52,5 @@ def test_batch_autotune_keeps_state():
     v = b.autotune(16)
     assert v == b.variant
     for i in range(len(members)):
-        assert np.array_equal(b.download(i), before[i])
+        assert bits_equal(b.download(i), before[i])
     b.close()

@@ -8,6 +8,7 @@ import pytest
 from formura_gb300 import workloads as W
 from formura_gb300.host import FormuraProgram, builtin_program
 from oracle.reference_lib import ReferenceProgram
+from conftest import bits_equal
 
 pytestmark = pytest.mark.gpu
 
@@ -23,11 +24,11 @@ def test_first_step_and_filter_bit_exact(extra, calls, tag):
     gpu = FormuraProgram(src, cfg, "smooth2d", name=f"smooth_{tag}_gpu")
     a, b = ref.init(), gpu.init()
     assert a == b
-    assert np.array_equal(ref.get("q"), gpu.get("q"))        # first_step applied in Init
+    assert bits_equal(ref.get("q"), gpu.get("q"))        # first_step applied in Init
     x = ref.get("q") + 0.01 * np.random.default_rng(4).standard_normal((64, 64))
     ref.set("q", x)
     gpu.set("q", x)
     for _ in range(calls):
         assert ref.forward(1) == gpu.forward(1)
-        assert np.array_equal(ref.get("q"), gpu.get("q"))
+        assert bits_equal(ref.get("q"), gpu.get("q"))
     gpu.finalize()

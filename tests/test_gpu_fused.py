@@ -8,6 +8,7 @@ import pytest
 
 from formura_gb300 import workloads as W
 from formura_gb300.host import Grid, builtin_program, program_uniforms
+from conftest import bits_equal
 
 pytestmark = pytest.mark.gpu
 
@@ -42,7 +43,7 @@ def test_every_variant_matches_single_steps(shape, prec):
             continue            # does not fit this device's shared memory
         g.forward(steps)
         got = g.download()
-        assert np.array_equal(got, ref), v
+        assert bits_equal(got, ref), v
     g.close()
 
 
@@ -56,7 +57,7 @@ def test_autotune_preserves_state_and_picks_a_variant():
     before = g.download()
     chosen = g.autotune(32)
     assert chosen >= -1 and g.variant == chosen
-    assert np.array_equal(g.download(), before)
+    assert bits_equal(g.download(), before)
     g.close()
 
 
@@ -103,6 +104,6 @@ def test_3d_streaming_variants_match_single_steps(shape, prec):
         tried += 1
         g.forward(steps)
         got = g.download()
-        assert np.array_equal(got, ref), v
+        assert bits_equal(got, ref), v
     assert tried >= 3
     g.close()

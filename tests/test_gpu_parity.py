@@ -12,6 +12,7 @@ import pytest
 from formura_gb300 import workloads as W
 from formura_gb300.host import FormuraProgram, builtin_program
 from oracle.reference_lib import ReferenceProgram
+from conftest import bits_equal
 
 pytestmark = pytest.mark.gpu
 
@@ -41,7 +42,7 @@ def test_heat_f64_bit_exact(n, steps, spf):
         gpu.forward(1)
     _check_navi(ref.navi_dict(), gpu.navi_dict())
     a, b = ref.get("q"), gpu.get("q")
-    assert np.array_equal(a, b), f"max |diff| {np.abs(a - b).max()}"
+    assert bits_equal(a, b), f"max |diff| {np.abs(a - b).max()}"
     gpu.finalize()
 
 
@@ -59,7 +60,7 @@ def test_heat_full_config_bit_exact():
     gpu.forward(1)
     _check_navi(ref.navi_dict(), gpu.navi_dict())
     a, b = ref.get("q"), gpu.get("q")
-    assert np.array_equal(a, b), f"rel-L2 {W.rel_l2(b, a)}"
+    assert bits_equal(a, b), f"rel-L2 {W.rel_l2(b, a)}"
     # the periodic explicit scheme conserves the total up to rounding
     assert abs(b.sum() - x.sum()) < 1e-9 * x.size
     gpu.finalize()
@@ -71,7 +72,7 @@ def test_gray_scott_f64_bit_exact(n, steps, spf):
     ref, gpu = _pair("gs2d", cfg, f"gpu_steps_per_forward: {spf}\n", f"n{n}s{spf}")
     _check_navi(ref.init(), gpu.init())
     for f in ("u", "v"):
-        assert np.array_equal(ref.get(f), gpu.get(f)), "init differs"
+        assert bits_equal(ref.get(f), gpu.get(f)), "init differs"
     st = W.gs_perturb(ref.get("u"), ref.get("v"), seed=7)
     for f in ("u", "v"):
         ref.set(f, st[f])
@@ -82,7 +83,7 @@ def test_gray_scott_f64_bit_exact(n, steps, spf):
     _check_navi(ref.navi_dict(), gpu.navi_dict())
     for f in ("u", "v"):
         a, b = ref.get(f), gpu.get(f)
-        assert np.array_equal(a, b), f"{f}: max |diff| {np.abs(a - b).max()}"
+        assert bits_equal(a, b), f"{f}: max |diff| {np.abs(a - b).max()}"
     gpu.finalize()
 
 
@@ -100,7 +101,7 @@ def test_gray_scott_4096_bit_exact_200_steps():
     gpu.forward(1)
     _check_navi(ref.navi_dict(), gpu.navi_dict())
     for f in ("u", "v"):
-        assert np.array_equal(ref.get(f), gpu.get(f))
+        assert bits_equal(ref.get(f), gpu.get(f))
     gpu.finalize()
 
 
@@ -149,7 +150,7 @@ def test_gpu_reproduces_reference_program_fixture(name, program):
     nav = gpu.forward(1)
     assert nav["offset_x"] == int(d["offset_x"]) and nav["time_step"] == int(d["time_step"])
     for f in gpu.fields:
-        assert np.array_equal(gpu.get(f), d["out_" + f]), f
+        assert bits_equal(gpu.get(f), d["out_" + f]), f
     gpu.finalize()
 
 
@@ -169,7 +170,7 @@ def test_hllc_f64_bit_exact_and_conservative():
     _check_navi(ref.navi_dict(), gpu.navi_dict())
     for f in ref.fields:
         a, b = ref.get(f), gpu.get(f)
-        assert np.array_equal(a, b), f"{f}: rel-L2 {W.rel_l2(b, a)}"
+        assert bits_equal(a, b), f"{f}: rel-L2 {W.rel_l2(b, a)}"
         # periodic flux-difference form conserves every total
         assert abs(b.sum() - st[f].sum()) <= 1e-10 * max(1.0, np.abs(st[f]).sum())
     gpu.finalize()
@@ -208,7 +209,7 @@ def test_hlld_f64_bit_exact():
         gpu.forward(1)
     _check_navi(ref.navi_dict(), gpu.navi_dict())
     for f in ref.fields:
-        assert np.array_equal(ref.get(f), gpu.get(f)), f
+        assert bits_equal(ref.get(f), gpu.get(f)), f
     gpu.finalize()
 
 
@@ -253,13 +254,13 @@ def test_sod_shock_tube_bit_exact_and_accurate():
     ref, gpu = _pair("sod1d", cfg, "", "sod")
     _check_navi(ref.init(), gpu.init())
     for f in ("e", "m", "rho"):
-        assert np.array_equal(ref.get(f), gpu.get(f))
+        assert bits_equal(ref.get(f), gpu.get(f))
     ref.forward(100)
     for _ in range(100):
         gpu.forward(1)
     _check_navi(ref.navi_dict(), gpu.navi_dict())
     for f in ("e", "m", "rho"):
-        assert np.array_equal(ref.get(f), gpu.get(f)), f
+        assert bits_equal(ref.get(f), gpu.get(f)), f
     d = np.load(os.path.join(os.path.dirname(__file__), "golden", "sod1d_t100.npz"))
     x, rho, u, pr = _sod_profile(gpu)
     sel = (x > 1.2) & (x < 2.8)
@@ -297,7 +298,66 @@ def test_two_grids_interleaved_match_sequential_runs():
     for _ in range(10):
         a.forward(3)
         b.forward(3)
-    assert np.array_equal(a.download(), alone[0])
-    assert np.array_equal(b.download(), alone[1])
+    assert bits_equal(a.download(), alone[0])
+    assert bits_equal(b.download(), alone[1])
     a.close()
     b.close()
+
+
+def _tiny(rng, shape, scale_exp):
+    """Values around 2^scale_exp (subnormal for scale_exp < -1022), a fifth
+    of them exact +0 and a fifth exact -0."""
+    x = rng.uniform(-1.0, 1.0, shape) * 2.0 ** scale_exp
+    r = rng.random(shape)
+    x[r < 0.2] = 0.0
+    x[(r >= 0.2) & (r < 0.4)] = -0.0
+    return x
+
+
+@pytest.mark.parametrize("program", ["heat3d", "gs2d", "sod1d", "hllc3d"])
+def test_tiny_values_and_signed_zeros_bit_exact(program):
+    """States with subnormal and tiny values and signed zeros, where the
+    shortened division and multiply-add forms of the exact policy must hand
+    over to the IEEE instructions: bit patterns (zero signs included) equal
+    to the oracle's after every call."""
+    rng = np.random.default_rng(11)
+    if program == "heat3d":
+        n = 12
+        cfg = W.heat_config(n)
+    elif program == "gs2d":
+        n = 32
+        cfg = W.gs_config(n)
+    elif program == "hllc3d":
+        n = 8
+        cfg = W.hllc_config(n)
+    else:
+        _, cfg = builtin_program(program)
+    ref, gpu = _pair(program, cfg, "", "tiny")
+    ref.init()
+    gpu.init()
+    shape = ref.get(ref.fields[0]).shape
+    st = {}
+    if program == "heat3d":
+        st["q"] = _tiny(rng, shape, -1030)
+        st["q"][:, :, : n // 2] = _tiny(rng, (n, n, n // 2), -950)
+    elif program == "gs2d":
+        st["u"] = 1.0 - 0.1 * rng.random(shape)
+        st["v"] = _tiny(rng, shape, -1040)
+        st["v"][: n // 2] = _tiny(rng, (n // 2, n), -960)
+        st["v"][n // 4: n // 2, n // 4: n // 2] = 0.25
+    else:
+        for f in ref.fields:
+            st[f] = ref.get(f).copy()
+        momenta = [f for f in ref.fields if f.startswith("m")]
+        for f in momenta:
+            st[f] = _tiny(rng, shape, -1030)
+            st[f].reshape(-1)[::3] = 0.1 * rng.uniform(-1, 1, st[f].reshape(-1)[::3].shape)
+    for f in ref.fields:
+        ref.set(f, st[f])
+        gpu.set(f, st[f])
+    for _ in range(6):
+        ref.forward(1)
+        gpu.forward(1)
+        for f in ref.fields:
+            assert bits_equal(ref.get(f), gpu.get(f)), f
+    gpu.finalize()
