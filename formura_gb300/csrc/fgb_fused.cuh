@@ -130,7 +130,7 @@ __device__ __forceinline__ void tile_steps(T* smem, const typename M::U* __restr
       for (int ly = lo + threadIdx.y; ly < RY - lo; ly += BY) {
         for (int lx = lo + threadIdx.x; lx < RX - lo; lx += BX) {
           TileAccess<T, NF, RY, RX> a{cur, nxt, ly, lx};
-          Stage::template run<M>(a, U);
+          eval<M, Stage>(a, U);
         }
       }
     } else {
@@ -141,7 +141,7 @@ __device__ __forceinline__ void tile_steps(T* smem, const typename M::U* __restr
 #pragma unroll
           for (int r = 0; r < RB; ++r) {
             RegTileAccess<T, NF, RY, RX> a{cur, res[r], min(ly0 + r, last), lx};
-            Stage::template run<M>(a, U);
+            eval<M, Stage>(a, U);
           }
 #pragma unroll
           for (int r = 0; r < RB; ++r) {
@@ -429,7 +429,7 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
           for (int lx = lo + threadIdx.x; lx < RX - lo; lx += BX) {
             T res[NF];
             PlaneAccess<T, NF, P, RY, RX> a{planes, ly * RX + lx, res};
-            Stage::template run<M>(a, U);
+            eval<M, Stage>(a, U);
 #pragma unroll
             for (int f = 0; f < NF; ++f) mine[(f * RY + ly) * RX + lx] = res[f];
           }
@@ -448,7 +448,7 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
             const int ox = small ? (px + K * Prog::kShift) % nx : pwrap(px + K * Prog::kShift, nx);
             T res[NF];
             PlaneAccess<T, NF, P, RY, RX> a{planes, (ty + HX) * RX + tx + HX, res};
-            Stage::template run<M>(a, U);
+            eval<M, Stage>(a, U);
             const size_t g = ((size_t)oz * ny + oy) * nx + ox;
 #pragma unroll
             for (int f = 0; f < NF; ++f)

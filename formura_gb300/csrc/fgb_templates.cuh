@@ -17,12 +17,25 @@ namespace fgb {
 // arithmetic policies
 // ---------------------------------------------------------------------------
 struct F64Fast;
+struct F64Ieee;
 
 // FP64, rounding exactly like the reference's C: one IEEE rounding per SSA
 // operation, no contraction (the __d*_rn intrinsics are never fused).
+//
+// Three operations take shortened forms that equal the reference's only
+// while no intermediate leaves the normal range: a multiply-add by a power
+// of two, a division by a grid-independent value through its host
+// reciprocal and a division through a shared reciprocal.  Each records on
+// the integer pipe whether its operands lie in its window (the `ok` flag of
+// the stage functor, which run() returns); a warp in which any lane's flag
+// dropped evaluates the functor again with F64Ieee, the plain separately
+// rounded operations (eval() below).  Inside the windows both give the same
+// bits, so the result never depends on which lanes share a warp.
 struct F64Exact {
   using T = double;
   using U = double;   // element type of the uniform table
+  using Ieee = F64Ieee;
+  static constexpr bool kChecked = true;
   // Arithmetic of the generated adjoint kernels: contracted FP64.  The
   // arrays an adjoint step recomputes for later stages keep this exact
   // policy, but the forward values a partial-sum kernel differentiates and
@@ -36,26 +49,19 @@ struct F64Exact {
   static __device__ __forceinline__ T mul(T a, T b) { return __dmul_rn(a, b); }
   static __device__ __forceinline__ T div(T a, T b) { return __ddiv_rn(a, b); }
 
-  // The shortened forms below equal the reference's separately rounded
-  // operations only while no intermediate leaves the normal range.  Each
-  // checks its operands' exponents on the integer pipe and takes a
-  // warp-uniform branch: a lane whose operands fall outside sends its warp
-  // to the plain IEEE instructions, so no lane issues both forms.
   static __device__ __forceinline__ uint64_t bits(T x) { return (uint64_t)__double_as_longlong(x); }
   static __device__ __forceinline__ unsigned expo(T x) { return (unsigned)(bits(x) >> 52) & 0x7ffu; }
   static __device__ __forceinline__ bool is_zero(T x) { return (bits(x) << 1) == 0; }
-  static __device__ __forceinline__ bool warp_all(bool ok) { return __all_sync(__activemask(), ok); }
   // biased exponent field within [1023 - w, 1023 + w]
   static __device__ __forceinline__ bool within(T x, unsigned w) { return expo(x) - (1023u - w) <= 2u * w; }
 
   // a*h + t for a = +-2^k (a literal): one rounding of the exact sum, which
   // is the reference's RN(RN(a*h) + t) as long as a*h is exact, that is h
   // is zero or a*h stays normal.
-  static __device__ __forceinline__ T fma(T a, T h, T t) {
+  static __device__ __forceinline__ T fma(T a, T h, T t, bool& ok) {
     const int k = (int)expo(a) - 1023;
-    const bool ok = is_zero(h) || (unsigned)((int)expo(h) + k - 1) <= 2045u;
-    if (warp_all(ok)) return __fma_rn(a, h, t);
-    return __dadd_rn(__dmul_rn(a, h), t);
+    ok &= is_zero(h) || (unsigned)((int)expo(h) + k - 1) <= 2045u;
+    return __fma_rn(a, h, t);
   }
   // q = RN(x / c) from y = RN(1 / c): Markstein's correction of RN(x * y),
   // exact when x - q*c is representable and q normal.  Zero numerators take
@@ -67,21 +73,22 @@ struct F64Exact {
   }
   // x / c for a grid-independent c with rc = RN(1/c) from the host:
   // numerators in [2^-900, 2^900] or zero, c in [2^-100, 2^100].
-  static __device__ __forceinline__ T divu(T x, T c, T rc) {
+  static __device__ __forceinline__ T divu(T x, T c, T rc, bool& ok) {
 #ifdef FGB_DIVU_IEEE
     (void)rc;
+    (void)ok;
     return __ddiv_rn(x, c);
 #else
-    if (warp_all(within(c, 100) && (is_zero(x) || within(x, 900)))) return markstein(x, c, rc);
-    return __ddiv_rn(x, c);
+    ok &= within(c, 100) && (is_zero(x) || within(x, 900));
+    return markstein(x, c, rc);
 #endif
   }
   // RN(1/b) for a grid value b that several quotients divide by
   static __device__ __forceinline__ T rcp(T b) { return __drcp_rn(b); }
   // a / b with y = rcp(b): operands in [2^-400, 2^400] (a may be zero)
-  static __device__ __forceinline__ T divr(T a, T b, T y) {
-    if (warp_all(within(b, 400) && (is_zero(a) || within(a, 400)))) return markstein(a, b, y);
-    return __ddiv_rn(a, b);
+  static __device__ __forceinline__ T divr(T a, T b, T y, bool& ok) {
+    ok &= within(b, 400) && (is_zero(a) || within(a, 400));
+    return markstein(a, b, y);
   }
   // The same operations on the integer pipes (fgb_softf64.h), with the
   // hardware instruction for the operands outside the fast path: the
@@ -110,24 +117,56 @@ struct F64Exact {
     if (__any_sync(__activemask(), !ok)) v = ok ? v : __dmul_rn(a, b);
     return v;
   }
-  static __device__ __forceinline__ T sfma(T c, T h, T t) {
+  static __device__ __forceinline__ T sfma(T c, T h, T t, bool& ok) {
     uint64_t r;
-    const bool ok = soft::scaled_add_bits(soft::to_bits(c), soft::to_bits(h), soft::to_bits(t), r);
+    const bool fast = soft::scaled_add_bits(soft::to_bits(c), soft::to_bits(h), soft::to_bits(t), r);
     T v = soft::from_bits(r);
-    if (__any_sync(__activemask(), !ok)) v = ok ? v : fma(c, h, t);
+    if (__any_sync(__activemask(), !fast)) v = fast ? v : fma(c, h, t, ok);
     return v;
   }
   // Markstein quotient with its first product on the integer pipes
-  static __device__ __forceinline__ T sdivu(T x, T c, T rc) {
+  static __device__ __forceinline__ T sdivu(T x, T c, T rc, bool& ok) {
 #ifdef FGB_DIVU_IEEE
     (void)rc;
+    (void)ok;
     return __ddiv_rn(x, c);
 #endif
-    if (!warp_all(within(c, 100) && (is_zero(x) || within(x, 900)))) return __ddiv_rn(x, c);
+    ok &= within(c, 100) && (is_zero(x) || within(x, 900));
     const T q = smul(x, rc);
     const T e = __fma_rn(-q, c, x);
     return is_zero(x) ? q : __fma_rn(e, rc, q);
   }
+  static __device__ __forceinline__ T neg(T a) { return -a; }
+  static __device__ __forceinline__ T sqrt(T a) { return __dsqrt_rn(a); }
+  static __device__ __forceinline__ T fabs(T a) { return ::fabs(a); }
+  static __device__ __forceinline__ T exp(T a) { return ::exp(a); }
+  static __device__ __forceinline__ T log(T a) { return ::log(a); }
+  static __device__ __forceinline__ T sin(T a) { return ::sin(a); }
+  static __device__ __forceinline__ T cos(T a) { return ::cos(a); }
+  static __device__ __forceinline__ T pow(T a, T b) { return ::pow(a, b); }
+};
+
+// The reference's separately rounded IEEE operations, without shortened
+// forms: what a warp of F64Exact falls back to.
+struct F64Ieee {
+  using T = double;
+  using U = double;
+  using Deriv = F64Fast;
+  using Ieee = F64Ieee;
+  static constexpr bool kChecked = false;
+  static __device__ __forceinline__ T add(T a, T b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ T sub(T a, T b) { return __dsub_rn(a, b); }
+  static __device__ __forceinline__ T mul(T a, T b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ T div(T a, T b) { return __ddiv_rn(a, b); }
+  static __device__ __forceinline__ T fma(T a, T h, T t, bool&) { return __dadd_rn(__dmul_rn(a, h), t); }
+  static __device__ __forceinline__ T divu(T x, T c, T, bool&) { return __ddiv_rn(x, c); }
+  static __device__ __forceinline__ T rcp(T b) { return __drcp_rn(b); }
+  static __device__ __forceinline__ T divr(T a, T b, T, bool&) { return __ddiv_rn(a, b); }
+  static __device__ __forceinline__ T sadd(T a, T b) { return __dadd_rn(a, b); }
+  static __device__ __forceinline__ T ssub(T a, T b) { return __dsub_rn(a, b); }
+  static __device__ __forceinline__ T smul(T a, T b) { return __dmul_rn(a, b); }
+  static __device__ __forceinline__ T sfma(T a, T h, T t, bool& ok) { return fma(a, h, t, ok); }
+  static __device__ __forceinline__ T sdivu(T x, T c, T rc, bool& ok) { return divu(x, c, rc, ok); }
   static __device__ __forceinline__ T neg(T a) { return -a; }
   static __device__ __forceinline__ T sqrt(T a) { return __dsqrt_rn(a); }
   static __device__ __forceinline__ T fabs(T a) { return ::fabs(a); }
@@ -143,19 +182,21 @@ struct F64Fast {
   using T = double;
   using U = double;
   using Deriv = F64Fast;
+  using Ieee = F64Fast;
+  static constexpr bool kChecked = false;
   static __device__ __forceinline__ T add(T a, T b) { return a + b; }
   static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
   static __device__ __forceinline__ T div(T a, T b) { return a / b; }
-  static __device__ __forceinline__ T fma(T a, T b, T c) { return ::fma(a, b, c); }
-  static __device__ __forceinline__ T divu(T x, T, T rc) { return x * rc; }
+  static __device__ __forceinline__ T fma(T a, T b, T c, bool&) { return ::fma(a, b, c); }
+  static __device__ __forceinline__ T divu(T x, T, T rc, bool&) { return x * rc; }
   static __device__ __forceinline__ T rcp(T b) { return __drcp_rn(b); }
-  static __device__ __forceinline__ T divr(T a, T, T y) { return a * y; }
+  static __device__ __forceinline__ T divr(T a, T, T y, bool&) { return a * y; }
   static __device__ __forceinline__ T sadd(T a, T b) { return a + b; }
   static __device__ __forceinline__ T ssub(T a, T b) { return a - b; }
   static __device__ __forceinline__ T smul(T a, T b) { return a * b; }
-  static __device__ __forceinline__ T sfma(T a, T b, T c) { return ::fma(a, b, c); }
-  static __device__ __forceinline__ T sdivu(T x, T, T rc) { return x * rc; }
+  static __device__ __forceinline__ T sfma(T a, T b, T c, bool&) { return ::fma(a, b, c); }
+  static __device__ __forceinline__ T sdivu(T x, T, T rc, bool&) { return x * rc; }
   static __device__ __forceinline__ T neg(T a) { return -a; }
   static __device__ __forceinline__ T sqrt(T a) { return ::sqrt(a); }
   static __device__ __forceinline__ T fabs(T a) { return ::fabs(a); }
@@ -175,21 +216,23 @@ struct F32 {
   using T = float;
   using U = float;
   using Deriv = F32;
+  using Ieee = F32;
+  static constexpr bool kChecked = false;
   static __device__ __forceinline__ T add(T a, T b) { return a + b; }
   static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
   // reciprocal-based quotient (2 ulp): the FP32 form trades the IEEE
   // division sequence for two instructions; its distance to FP64 is reported
   static __device__ __forceinline__ T div(T a, T b) { return __fdividef(a, b); }
-  static __device__ __forceinline__ T fma(T a, T b, T c) { return fmaf(a, b, c); }
-  static __device__ __forceinline__ T divu(T x, T, T rc) { return x * rc; }
+  static __device__ __forceinline__ T fma(T a, T b, T c, bool&) { return fmaf(a, b, c); }
+  static __device__ __forceinline__ T divu(T x, T, T rc, bool&) { return x * rc; }
   static __device__ __forceinline__ T rcp(T b) { return __fdividef(1.0f, b); }
-  static __device__ __forceinline__ T divr(T a, T, T y) { return a * y; }
+  static __device__ __forceinline__ T divr(T a, T, T y, bool&) { return a * y; }
   static __device__ __forceinline__ T sadd(T a, T b) { return a + b; }
   static __device__ __forceinline__ T ssub(T a, T b) { return a - b; }
   static __device__ __forceinline__ T smul(T a, T b) { return a * b; }
-  static __device__ __forceinline__ T sfma(T a, T b, T c) { return fmaf(a, b, c); }
-  static __device__ __forceinline__ T sdivu(T x, T, T rc) { return x * rc; }
+  static __device__ __forceinline__ T sfma(T a, T b, T c, bool&) { return fmaf(a, b, c); }
+  static __device__ __forceinline__ T sdivu(T x, T, T rc, bool&) { return x * rc; }
   static __device__ __forceinline__ T neg(T a) { return -a; }
   static __device__ __forceinline__ T sqrt(T a) { return sqrtf(a); }
   static __device__ __forceinline__ T fabs(T a) { return fabsf(a); }
@@ -333,6 +376,20 @@ struct AdjointAccess {
 
 constexpr int kBlockX = 128;
 
+// One evaluation of a stage functor at the access's point.  In the
+// bit-faithful FP64 policy a warp in which any lane met an operand outside a
+// shortened form's window evaluates the functor again with the plain IEEE
+// operations: it reads the same inputs and overwrites the same outputs.
+template <class M, class F, class A>
+__device__ __forceinline__ void eval(const A& a, const typename M::U* __restrict__ U) {
+  const bool ok = F::template run<M>(a, U);
+  if constexpr (M::kChecked) {
+    if (__any_sync(__activemask(), !ok)) F::template run<typename M::Ieee>(a, U);
+  } else {
+    (void)ok;
+  }
+}
+
 // One thread per grid point of RPT consecutive rows (the middle axis); x
 // covers the contiguous (last) axis.  With RPT > 1 a thread has the loads of
 // several points in flight at once, which is what a memory-bound FP32/FP16
@@ -346,7 +403,7 @@ __global__ void __launch_bounds__(kBlockX) stage_kernel(const __grid_constant__ 
     const int p1 = (int)blockIdx.y * RPT + r;
     if (RPT > 1 && p1 >= L.n[1]) break;
     GlobalAccess<S, typename M::T, DIM, SHIFT> a{L, (int)blockIdx.z, p1, p2};
-    Stage::template run<M>(a, static_cast<const typename M::U*>(L.uniforms));
+    eval<M, Stage>(a, static_cast<const typename M::U*>(L.uniforms));
   }
 }
 
@@ -359,7 +416,7 @@ __global__ void __launch_bounds__(kBlockX) adjoint_kernel(const __grid_constant_
     const int p1 = (int)blockIdx.y * RPT + r;
     if (RPT > 1 && p1 >= L.n[1]) break;
     AdjointAccess<S, typename M::T> a{L, (int)blockIdx.z, p1, p2};
-    Adj::template run<M>(a, static_cast<const typename M::U*>(L.uniforms));
+    eval<M, Adj>(a, static_cast<const typename M::U*>(L.uniforms));
   }
 }
 
@@ -582,7 +639,7 @@ __global__ void __launch_bounds__(kBlockX) adj_stage_kernel(const __grid_constan
   const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
   if (p2 >= L.n[2]) return;
   Acc a{L, (int)blockIdx.z, (int)blockIdx.y, p2};
-  F::template run<M>(a, static_cast<const typename M::U*>(L.uniforms));
+  eval<M, F>(a, static_cast<const typename M::U*>(L.uniforms));
 }
 
 template <class Prog, int P, class F, bool Gather>

@@ -270,8 +270,9 @@ def emit_adjoint(mm: MMProgram, name: str, pe: _ProgramEmitter = None):
     body = "\n".join("    " + l.strip() for l in lines) + "\n" + "\n".join(out)
     return (f"struct AdjointStep {{\n"
             f"  template <class M, class A>\n"
-            f"  static __device__ __forceinline__ void run(const A& a, const typename M::U* __restrict__ U) {{\n"
-            f"    using T = typename M::T;\n    using D = typename M::Deriv;\n    (void)U;\n{body}\n  }}\n}};\n"), pe
+            f"  static __device__ __forceinline__ bool run(const A& a, const typename M::U* __restrict__ U) {{\n"
+            f"    using T = typename M::T;\n    using D = typename M::Deriv;\n    bool fgb_ok = true;\n"
+            f"    (void)U;\n{body}\n    return fgb_ok;\n  }}\n}};\n"), pe
 
 
 # ---------------------------------------------------------------------------
@@ -454,8 +455,9 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
             part_names.append(name)
             texts.append(f"struct {name} {{\n"
                          f"  template <class M, class A>\n"
-                         f"  static __device__ __forceinline__ void run(const A& a, const typename M::U* __restrict__ U) {{\n"
-                         f"    using T = typename M::T;\n    using D = typename M::Deriv;\n    (void)U;\n{body}\n  }}\n}};\n")
+                         f"  static __device__ __forceinline__ bool run(const A& a, const typename M::U* __restrict__ U) {{\n"
+                         f"    using T = typename M::T;\n    using D = typename M::Deriv;\n    bool fgb_ok = true;\n"
+                         f"    (void)U;\n{body}\n    return fgb_ok;\n  }}\n}};\n")
         pair_lists.append(pairs)
         direct = "true" if _stage_is_linear(an, st) else "false"
         texts.append(f"struct AdjStage{st.index} {{\n"
@@ -488,8 +490,9 @@ def emit_stage_adjoints(pe: _ProgramEmitter):
                     lines.append(f"    a.template accs<{g}, true>(T(0));")
         gathers[st.index] = (f"struct AdjGather{st.index} {{\n"
                              f"  template <class M, class A>\n"
-                             f"  static __device__ __forceinline__ void run(const A& a, const typename M::U* __restrict__ U) {{\n"
-                             f"    using T = typename M::T;\n    (void)U;\n" + "\n".join(lines) + "\n  }\n};\n")
+                             f"  static __device__ __forceinline__ bool run(const A& a, const typename M::U* __restrict__ U) {{\n"
+                             f"    using T = typename M::T;\n    (void)U;\n" + "\n".join(lines) +
+                             "\n    return true;\n  }\n};\n")
     # the stages an adjoint step recomputes: those whose arrays the partial
     # sums read, and the stages those depend on
     producer = {pe.mids.index(m): s.index for s in pe.stages for m in s.mid_out}

@@ -472,10 +472,10 @@ class _StageEmitter:
             if op in ("+", "-"):
                 if b[0] == "scaled":
                     c = b[1] if op == "+" else -b[1]
-                    return self.bind(f"{self.P}::fma(T({c_double(c)}), {self.as_T(b[2])}, {self.as_T(a)})")
+                    return self.bind(f"{self.P}::fma(T({c_double(c)}), {self.as_T(b[2])}, {self.as_T(a)}, fgb_ok)")
                 if a[0] == "scaled":
                     rhs = self.as_T(b) if op == "+" else f"{self.P}::neg({self.as_T(b)})"
-                    return self.bind(f"{self.P}::fma(T({c_double(a[1])}), {self.as_T(a[2])}, {rhs})")
+                    return self.bind(f"{self.P}::fma(T({c_double(a[1])}), {self.as_T(a[2])}, {rhs}, fgb_ok)")
                 fn = "add" if op == "+" else "sub"
                 return self.bind(f"{self.P}::{fn}({self.as_T(a)}, {self.as_T(b)})")
             if op == "/":
@@ -484,7 +484,7 @@ class _StageEmitter:
                     if b[0] == "lit" and is_pow2(b[1]):
                         return self.bind(f"{self.P}::mul({self.as_T(a)}, T({c_double(1.0 / b[1])}))")
                     rc = self.recip_handle(dep)
-                    return self.bind(f"{self.P}::divu({self.as_T(a)}, {self.as_T(b)}, {self.as_T(rc)})")
+                    return self.bind(f"{self.P}::divu({self.as_T(a)}, {self.as_T(b)}, {self.as_T(rc)}, fgb_ok)")
                 if self.reciprocal:
                     r = self.bind(f"{self.P}::div(T(1), {self.as_T(b)})")
                     return self.bind(f"{self.P}::mul({self.as_T(a)}, {self.as_T(r)})")
@@ -492,7 +492,7 @@ class _StageEmitter:
                 self.div_seen[den] = self.div_seen.get(den, 0) + 1
                 if self.div_uses.get(den, 0) >= 2:
                     y = self.bind(f"{self.P}::rcp({den})", prefix="r")
-                    return self.bind(f"{self.P}::divr({self.as_T(a)}, {den}, {self.as_T(y)})")
+                    return self.bind(f"{self.P}::divr({self.as_T(a)}, {den}, {self.as_T(y)}, fgb_ok)")
                 return self.bind(f"{self.P}::div({self.as_T(a)}, {den})")
             if op == "**":
                 if b[0] == "lit" and b[1] == 2.0:
@@ -623,9 +623,10 @@ class _ProgramEmitter:
 
                 f"  static constexpr int kMidOut = {len(st.mid_out)};\n"
                 f"  template <class M, class A>\n"
-                f"  static __device__ __forceinline__ void run(const A& a, const typename M::U* __restrict__ U) {{\n"
+                f"  static __device__ __forceinline__ bool run(const A& a, const typename M::U* __restrict__ U) {{\n"
                 f"    using T = typename M::T;\n"
-                f"    (void)U;\n{body}\n  }}\n}};\n")
+                f"    bool fgb_ok = true;\n"
+                f"    (void)U;\n{body}\n    return fgb_ok;\n  }}\n}};\n")
         adj_src = None
         stage_adj = None
         if self.graph == "step" and len(self.stages) == 1 and not self.mids:

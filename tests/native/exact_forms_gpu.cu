@@ -1,14 +1,14 @@
 // GPU check of the shortened operations of the bit-faithful FP64 policy
 // (fgb::F64Exact::divu, ::divr with ::rcp, ::fma with a power-of-two factor)
-// against the reference's separately rounded IEEE operations, bit for bit.
-// Operand classes are chosen per warp, so that warps whose lanes all lie in
-// the shortened forms' range take them, and others (subnormal, tiny, huge,
-// infinite or NaN operands, signed zeros) take the fallback, alone or mixed.
+// against the reference's separately rounded IEEE operations, bit for bit,
+// wherever the form's range flag stays set.  Operand classes: moderate, wide,
+// subnormal and tiny, huge and non-finite, signed zeros, any bit pattern.
 #include <cuda_runtime.h>
 #include <stdint.h>
 #include "../../formura_gb300/csrc/fgb_templates.cuh"
 
 using fgb::F64Exact;
+using fgb::F64Ieee;
 
 __device__ __forceinline__ uint64_t mix(uint64_t x) {
   // splitmix64 finaliser
@@ -42,8 +42,11 @@ __device__ __forceinline__ bool same(double a, double b) {
   return __double_as_longlong(a) == __double_as_longlong(b) || (a != a && b != b);
 }
 
+// A shortened form whose flag stays set must give the IEEE result's bits;
+// where the flag drops, the kernels evaluate with F64Ieee instead.  Counts
+// per operation: mismatches with the flag set, and lanes with the flag set.
 __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
-  unsigned long long bad[3] = {0, 0, 0};
+  unsigned long long bad[3] = {0, 0, 0}, fast[3] = {0, 0, 0};
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
     const uint64_t key = seed * 0x100000000ull + i;
@@ -53,27 +56,39 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
     const double c = operand(warp * 11 + seed, ca == 3 ? 1 : ca % 2);
     const double rc = 1.0 / c;
     const double x = operand(key * 7 + 1, cb == 5 ? (int)(mix(key) % 6) : cb);
-    if (!same(F64Exact::divu(x, c, rc), __ddiv_rn(x, c))) ++bad[0];
+    bool ok = true;
+    double r = F64Exact::divu(x, c, rc, ok);
+    fast[0] += ok;
+    bad[0] += ok && !same(r, __ddiv_rn(x, c));
     // divr: grid numerator and denominator
     const double a = operand(key * 7 + 2, ca == 5 ? (int)(mix(key ^ 1) % 6) : ca);
     const double b = operand(key * 7 + 3, cb);
-    if (!same(F64Exact::divr(a, b, F64Exact::rcp(b)), __ddiv_rn(a, b))) ++bad[1];
+    ok = true;
+    r = F64Exact::divr(a, b, F64Exact::rcp(b), ok);
+    fast[1] += ok;
+    bad[1] += ok && !same(r, __ddiv_rn(a, b));
     // fma with a = +-2^k, k in [-3, 3]: RN(RN(a*h) + t)
     const int k = (int)(mix(warp * 7 + seed) % 7) - 3;
     const double f = ((warp & 1) ? -1.0 : 1.0) * ldexp(1.0, k);
     const double h = operand(key * 7 + 4, cb), t = operand(key * 7 + 5, (cb + 1) % 6);
-    if (!same(F64Exact::fma(f, h, t), __dadd_rn(__dmul_rn(f, h), t))) ++bad[2];
+    ok = true;
+    r = F64Exact::fma(f, h, t, ok);
+    fast[2] += ok;
+    bad[2] += ok && !same(r, __dadd_rn(__dmul_rn(f, h), t));
   }
-  for (int j = 0; j < 3; ++j) atomicAdd(&out[j], bad[j]);
+  for (int j = 0; j < 3; ++j) {
+    atomicAdd(&out[j], bad[j]);
+    atomicAdd(&out[3 + j], fast[j]);
+  }
 }
 
 extern "C" int exact_forms_gpu_check(unsigned long long seed, unsigned long long n, unsigned long long* host_out) {
   unsigned long long* d = nullptr;
-  if (cudaMalloc(&d, 3 * sizeof(unsigned long long)) != cudaSuccess) return 1;
-  cudaMemset(d, 0, 3 * sizeof(unsigned long long));
+  if (cudaMalloc(&d, 6 * sizeof(unsigned long long)) != cudaSuccess) return 1;
+  cudaMemset(d, 0, 6 * sizeof(unsigned long long));
   check<<<152 * 8, 256>>>(seed, n, d);
   cudaError_t e = cudaDeviceSynchronize();
-  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 3 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
   cudaFree(d);
   return e == cudaSuccess ? 0 : 2;
 }

@@ -43,15 +43,17 @@ struct Exact {
   static T sub(T a, T b) { return a - b; }
   static T mul(T a, T b) { return a * b; }
   static T div(T a, T b) { return a / b; }
-  static T fma(T a, T b, T c) { return std::fma(a, b, c); }   // a is a power of two: exact product
-  static T divu(T x, T c, T) { return x / c; }                // the device's corrected quotient is this
+  // the reference's separately rounded operations, which the device's
+  // shortened forms (or their IEEE fallback) reproduce
+  static T fma(T a, T b, T c, bool&) { return a * b + c; }
+  static T divu(T x, T c, T, bool&) { return x / c; }
   static T rcp(T b) { return 1.0 / b; }
-  static T divr(T a, T b, T) { return a / b; }                // likewise
+  static T divr(T a, T b, T, bool&) { return a / b; }
   static T sadd(T a, T b) { return a + b; }
   static T ssub(T a, T b) { return a - b; }
   static T smul(T a, T b) { return a * b; }
-  static T sfma(T a, T b, T c) { return std::fma(a, b, c); }
-  static T sdivu(T x, T c, T) { return x / c; }
+  static T sfma(T a, T b, T c, bool&) { return a * b + c; }
+  static T sdivu(T x, T c, T, bool&) { return x / c; }
   static T neg(T a) { return -a; }
   static T sqrt(T a) { return std::sqrt(a); }
   static T fabs(T a) { return std::fabs(a); }

@@ -2,8 +2,9 @@
 (division by a grid-independent constant through its host reciprocal, a
 quotient through a shared reciprocal, a multiply-add by a power of two)
 against the reference's separately rounded IEEE operations: bit for bit on
-2^28 operands per seed, including subnormal, tiny, huge and non-finite
-operands and signed zeros, where they fall back to the IEEE instructions."""
+2^28 operands per seed wherever their range flag stays set; the operands
+include subnormal, tiny, huge and non-finite values and signed zeros, for
+which the flag drops and the kernels use the IEEE operations."""
 import ctypes
 import os
 import subprocess
@@ -29,6 +30,10 @@ def lib(tmp_path_factory):
 
 @pytest.mark.parametrize("seed", [1, 2, 3])
 def test_exact_forms_match_ieee(lib, seed):
-    out = (ctypes.c_ulonglong * 3)()
-    assert lib.exact_forms_gpu_check(seed, 2**28, out) == 0
-    assert list(out) == [0, 0, 0], ("divu, divr, fma mismatches", list(out))
+    n = 2**28
+    out = (ctypes.c_ulonglong * 6)()
+    assert lib.exact_forms_gpu_check(seed, n, out) == 0
+    bad, fast = list(out[:3]), list(out[3:])
+    assert bad == [0, 0, 0], ("divu, divr, fma mismatches with the range flag set", bad)
+    # the shortened forms apply to most operands, and not to all of them
+    assert all(0.3 * n < f < n for f in fast), fast
