@@ -49,9 +49,22 @@ struct F64Exact {
   static __device__ __forceinline__ T mul(T a, T b) { return __dmul_rn(a, b); }
   static __device__ __forceinline__ T div(T a, T b) { return __ddiv_rn(a, b); }
 
-  static __device__ __forceinline__ uint64_t bits(T x) { return (uint64_t)__double_as_longlong(x); }
-  static __device__ __forceinline__ unsigned expo(T x) { return (unsigned)(bits(x) >> 52) & 0x7ffu; }
-  static __device__ __forceinline__ bool is_zero(T x) { return (bits(x) << 1) == 0; }
+  // The range checks read the two 32-bit halves through an opaque move, so
+  // that the compiler keeps them on the integer pipe instead of turning a
+  // bit test into an FP64 comparison on the (busy) FP64 pipe.
+  static __device__ __forceinline__ void halves(T x, unsigned& lo, unsigned& hi) {
+    asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(x));
+  }
+  static __device__ __forceinline__ unsigned expo(T x) {
+    unsigned lo, hi;
+    halves(x, lo, hi);
+    return (hi >> 20) & 0x7ffu;
+  }
+  static __device__ __forceinline__ bool is_zero(T x) {
+    unsigned lo, hi;
+    halves(x, lo, hi);
+    return ((hi << 1) | lo) == 0u;
+  }
   // biased exponent field within [1023 - w, 1023 + w]
   static __device__ __forceinline__ bool within(T x, unsigned w) { return expo(x) - (1023u - w) <= 2u * w; }
 
@@ -59,7 +72,7 @@ struct F64Exact {
   // is the reference's RN(RN(a*h) + t) as long as a*h is exact, that is h
   // is zero or a*h stays normal.
   static __device__ __forceinline__ T fma(T a, T h, T t, bool& ok) {
-    const int k = (int)expo(a) - 1023;
+    const int k = (int)(((unsigned long long)__double_as_longlong(a) >> 52) & 0x7ffu) - 1023;   // a literal
     ok &= is_zero(h) || (unsigned)((int)expo(h) + k - 1) <= 2045u;
     return __fma_rn(a, h, t);
   }
