@@ -25,12 +25,15 @@ struct F64Ieee;
 // Three operations take shortened forms that equal the reference's only
 // while no intermediate leaves the normal range: a multiply-add by a power
 // of two, a division by a grid-independent value through its host
-// reciprocal and a division through a shared reciprocal.  Each records on
-// the integer pipe whether its operands lie in its window (the `ok` flag of
-// the stage functor, which run() returns); a warp in which any lane's flag
-// dropped evaluates the functor again with F64Ieee, the plain separately
-// rounded operations (eval() below).  Inside the windows both give the same
-// bits, so the result never depends on which lanes share a warp.
+// reciprocal and a division through a shared reciprocal.  Each checks on the
+// integer pipe whether its operands lie in its window.  The divisions take a
+// warp-uniform branch to the IEEE division when a lane's operands do not;
+// the multiply-add, whose window is left only near overflow or underflow,
+// records it in the `ok` flag of the stage functor (which run() returns),
+// and a warp in which any lane's flag dropped evaluates the functor again
+// with F64Ieee, the plain separately rounded operations (eval() below).
+// Inside the windows both forms give the same bits, so the result never
+// depends on which lanes share a warp.
 struct F64Exact {
   using T = double;
   using U = double;   // element type of the uniform table
@@ -84,24 +87,28 @@ struct F64Exact {
     const T e = __fma_rn(-q, c, x);
     return is_zero(x) ? q : __fma_rn(e, y, q);
   }
+  // The divisions decide per operation instead of raising the flag: a field
+  // that decays through the subnormal range (Gray-Scott's v far from the
+  // pattern) keeps whole warps out of the window for many steps, and there
+  // one IEEE division costs less than evaluating the stage twice.
+  static __device__ __forceinline__ bool warp_all(bool ok) { return __all_sync(__activemask(), ok); }
   // x / c for a grid-independent c with rc = RN(1/c) from the host:
   // numerators in [2^-900, 2^900] or zero, c in [2^-100, 2^100].
-  static __device__ __forceinline__ T divu(T x, T c, T rc, bool& ok) {
+  static __device__ __forceinline__ T divu(T x, T c, T rc, bool&) {
 #ifdef FGB_DIVU_IEEE
     (void)rc;
-    (void)ok;
     return __ddiv_rn(x, c);
 #else
-    ok &= within(c, 100) && (is_zero(x) || within(x, 900));
-    return markstein(x, c, rc);
+    if (warp_all(within(c, 100) && (is_zero(x) || within(x, 900)))) return markstein(x, c, rc);
+    return __ddiv_rn(x, c);
 #endif
   }
   // RN(1/b) for a grid value b that several quotients divide by
   static __device__ __forceinline__ T rcp(T b) { return __drcp_rn(b); }
   // a / b with y = rcp(b): operands in [2^-400, 2^400] (a may be zero)
-  static __device__ __forceinline__ T divr(T a, T b, T y, bool& ok) {
-    ok &= within(b, 400) && (is_zero(a) || within(a, 400));
-    return markstein(a, b, y);
+  static __device__ __forceinline__ T divr(T a, T b, T y, bool&) {
+    if (warp_all(within(b, 400) && (is_zero(a) || within(a, 400)))) return markstein(a, b, y);
+    return __ddiv_rn(a, b);
   }
   // The same operations on the integer pipes (fgb_softf64.h), with the
   // hardware instruction for the operands outside the fast path: the
@@ -138,13 +145,12 @@ struct F64Exact {
     return v;
   }
   // Markstein quotient with its first product on the integer pipes
-  static __device__ __forceinline__ T sdivu(T x, T c, T rc, bool& ok) {
+  static __device__ __forceinline__ T sdivu(T x, T c, T rc, bool&) {
 #ifdef FGB_DIVU_IEEE
     (void)rc;
-    (void)ok;
     return __ddiv_rn(x, c);
 #endif
-    ok &= within(c, 100) && (is_zero(x) || within(x, 900));
+    if (!warp_all(within(c, 100) && (is_zero(x) || within(x, 900)))) return __ddiv_rn(x, c);
     const T q = smul(x, rc);
     const T e = __fma_rn(-q, c, x);
     return is_zero(x) ? q : __fma_rn(e, rc, q);
