@@ -92,22 +92,31 @@ struct F64Exact {
   // pattern) keeps whole warps out of the window for many steps, and there
   // one IEEE division costs less than evaluating the stage twice.
   static __device__ __forceinline__ bool warp_all(bool ok) { return __all_sync(__activemask(), ok); }
-  // x / c for a grid-independent c with rc = RN(1/c) from the host:
-  // numerators in [2^-900, 2^900] or zero, c in [2^-100, 2^100].
+  // x / c for a grid-independent c with rc = RN(1/c) from the host: c in
+  // [2^-100, 2^100]; x zero, or of exponent in [-960, 960] with the
+  // quotient's exponent in [-1000, 1000] (then x - q*c is representable and
+  // q normal)
+  static __device__ __forceinline__ bool divu_window(T x, T c) {
+    const unsigned ex = expo(x);
+    return within(c, 100) && (is_zero(x) || (ex - 63u <= 1920u && ex - expo(c) + 1000u <= 2000u));
+  }
   static __device__ __forceinline__ T divu(T x, T c, T rc, bool&) {
 #ifdef FGB_DIVU_IEEE
     (void)rc;
     return __ddiv_rn(x, c);
 #else
-    if (warp_all(within(c, 100) && (is_zero(x) || within(x, 900)))) return markstein(x, c, rc);
+    if (warp_all(divu_window(x, c))) return markstein(x, c, rc);
     return __ddiv_rn(x, c);
 #endif
   }
   // RN(1/b) for a grid value b that several quotients divide by
   static __device__ __forceinline__ T rcp(T b) { return __drcp_rn(b); }
   // a / b with y = rcp(b): operands in [2^-400, 2^400] (a may be zero)
+  static __device__ __forceinline__ bool divr_window(T a, T b) {
+    return within(b, 400) && (is_zero(a) || within(a, 400));
+  }
   static __device__ __forceinline__ T divr(T a, T b, T y, bool&) {
-    if (warp_all(within(b, 400) && (is_zero(a) || within(a, 400)))) return markstein(a, b, y);
+    if (warp_all(divr_window(a, b))) return markstein(a, b, y);
     return __ddiv_rn(a, b);
   }
   // The same operations on the integer pipes (fgb_softf64.h), with the
@@ -150,7 +159,7 @@ struct F64Exact {
     (void)rc;
     return __ddiv_rn(x, c);
 #endif
-    if (!warp_all(within(c, 100) && (is_zero(x) || within(x, 900)))) return __ddiv_rn(x, c);
+    if (!warp_all(divu_window(x, c))) return __ddiv_rn(x, c);
     const T q = smul(x, rc);
     const T e = __fma_rn(-q, c, x);
     return is_zero(x) ? q : __fma_rn(e, rc, q);

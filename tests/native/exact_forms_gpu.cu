@@ -59,14 +59,14 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
     const double x = operand(key * 7 + 1, cb == 5 ? (int)(mix(key) % 6) : cb);
     bool ok = true;
     double r = F64Exact::divu(x, c, rc, ok);
-    fast[0] += F64Exact::within(c, 100) && (F64Exact::is_zero(x) || F64Exact::within(x, 900));
+    fast[0] += F64Exact::divu_window(x, c);
     bad[0] += ok && !same(r, __ddiv_rn(x, c));
     // divr: grid numerator and denominator
     const double a = operand(key * 7 + 2, ca == 5 ? (int)(mix(key ^ 1) % 6) : ca);
     const double b = operand(key * 7 + 3, cb);
     ok = true;
     r = F64Exact::divr(a, b, F64Exact::rcp(b), ok);
-    fast[1] += F64Exact::within(b, 400) && (F64Exact::is_zero(a) || F64Exact::within(a, 400));
+    fast[1] += F64Exact::divr_window(a, b);
     bad[1] += ok && !same(r, __ddiv_rn(a, b));
     // fma with a = +-2^k, k in [-3, 3]: RN(RN(a*h) + t)
     const int k = (int)(mix(warp * 7 + seed) % 7) - 3;

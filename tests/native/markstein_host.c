@@ -3,6 +3,9 @@
  * fma), result RN(q + e*y), or q itself for a zero numerator.  Inside the
  * windows the result must equal RN(a/b) bit for bit; just below them (tiny
  * numerators) it need not, which is why the device falls back there.
+ * The windows: for a grid-independent c in [2^-100, 2^100], numerators of
+ * exponent in [-960, 960] whose quotient's exponent is in [-1000, 1000];
+ * for a shared reciprocal, both operands in [2^-400, 2^400].
  * Uses the host's correctly rounded fma.  Prints "mismatches_inside outside". */
 #include <math.h>
 #include <stdint.h>
@@ -32,9 +35,12 @@ int main(int argc, char** argv) {
   long n = argc > 1 ? atol(argv[1]) : 10000000;
   long inside = 0, outside = 0;
   for (long i = 0; i < n; ++i) {
-    /* divisions by constants: numerator window [2^-900, 2^900], c in [2^-100, 2^100] */
+    /* divisions by constants: c in [2^-100, 2^100], numerator exponent in
+       [-960, 960] with the quotient's exponent in [-1000, 1000] */
     double c = mant_operand(1023 - 100, 1023 + 100, (int)(i % 3));
-    double x = (i % 50 == 0) ? from((rnd() & 1) << 63) : mant_operand(1023 - 900, 1023 + 900, (int)(i % 3));
+    int ec = (int)((bits(c) >> 52) & 0x7ff) - 1023;
+    int lo = -960 > ec - 1000 ? -960 : ec - 1000, hi = 960 < ec + 1000 ? 960 : ec + 1000;
+    double x = (i % 50 == 0) ? from((rnd() & 1) << 63) : mant_operand(1023 + lo, 1023 + hi, (int)(i % 3));
     double r = corrected(x, c, 1.0 / c), w = x / c;
     inside += bits(r) != bits(w);
     /* shared reciprocals: both operands in [2^-400, 2^400] */
@@ -45,6 +51,19 @@ int main(int argc, char** argv) {
     inside += bits(r) != bits(w);
     /* below the window: subnormal and lowest normal numerators */
     double t = from(((rnd() & 1) << 63) | ((rnd() % 40) << 52) | (rnd() & 0x000fffffffffffffull));
+    /* the lowest exponents of the window, against the smallest constants */
+    double c2 = mant_operand(1023 - 100, 1023 - 90, (int)(i % 3));
+    double x2 = mant_operand(1023 - 960, 1023 - 950, (int)((i / 3) % 3));
+    r = corrected(x2, c2, 1.0 / c2);
+    w = x2 / c2;
+    inside += bits(r) != bits(w);
+    /* the quotient's lowest exponents: large constants, small numerators */
+    double c3 = mant_operand(1023 + 90, 1023 + 100, (int)(i % 3));
+    int e3 = (int)((bits(c3) >> 52) & 0x7ff) - 1023;
+    double x3 = mant_operand(1023 + e3 - 1000, 1023 + e3 - 990, (int)((i / 3) % 3));
+    r = corrected(x3, c3, 1.0 / c3);
+    w = x3 / c3;
+    inside += bits(r) != bits(w);
     r = corrected(t, c, 1.0 / c);
     w = t / c;
     outside += bits(r) != bits(w);
