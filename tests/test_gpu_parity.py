@@ -361,3 +361,31 @@ def test_tiny_values_and_signed_zeros_bit_exact(program):
         for f in ref.fields:
             assert bits_equal(ref.get(f), gpu.get(f)), f
     gpu.finalize()
+
+
+def test_gray_scott_decay_through_subnormals_bit_exact():
+    """Gray-Scott without a pattern: v decays by about e^-0.1 per step, so a
+    field of +-1e-300 enters the subnormal range after some 180 steps (the
+    regime of the 4096^2 run's far field after some 7000 steps).
+    The state after every 50 steps equals the oracle's bit for bit."""
+    n = 64
+    cfg = W.gs_config(n)
+    ref, gpu = _pair("gs2d", cfg, "gpu_steps_per_forward: 50\n", "decay")
+    ref.init()
+    gpu.init()
+    rng = np.random.default_rng(5)
+    u = 1.0 - 0.01 * rng.random((n, n))
+    v = 1e-300 * rng.uniform(-1.0, 1.0, (n, n))
+    for f, x in (("u", u), ("v", v)):
+        ref.set(f, x)
+        gpu.set(f, x)
+    subnormal_seen = False
+    for _ in range(8):
+        ref.forward(50)
+        gpu.forward(1)
+        a = ref.get("v")
+        subnormal_seen |= bool(((a != 0) & (np.abs(a) < 2.2250738585072014e-308)).any())
+        for f in ("u", "v"):
+            assert bits_equal(ref.get(f), gpu.get(f)), f
+    assert subnormal_seen
+    gpu.finalize()
