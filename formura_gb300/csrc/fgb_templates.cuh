@@ -422,14 +422,11 @@ __device__ __forceinline__ void eval(const A& a, const typename M::U* __restrict
 // covers the contiguous (last) axis.  With RPT > 1 a thread has the loads of
 // several points in flight at once, which is what a memory-bound FP32/FP16
 // step needs to cover the HBM latency.
-// blocks per SM the one-step kernels are compiled for (a register cap for
-// the large FP64 stages; 1 leaves the choice to the compiler)
-#ifndef FGB_STAGE_MIN_BLOCKS
-#define FGB_STAGE_MIN_BLOCKS 1
-#endif
-
+// (Capping the large FP64 stages' registers for more resident blocks was
+// measured and lost: HLLD FP64 0.212 GLUP/s uncapped, 0.203 at 128
+// registers, 0.193 at 102.)
 template <class M, class S, int DIM, int SHIFT, class Stage, int RPT>
-__global__ void __launch_bounds__(kBlockX, FGB_STAGE_MIN_BLOCKS) stage_kernel(const __grid_constant__ FgbLaunch L) {
+__global__ void __launch_bounds__(kBlockX) stage_kernel(const __grid_constant__ FgbLaunch L) {
   const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
   if (p2 >= L.n[2]) return;
 #pragma unroll
