@@ -100,11 +100,20 @@ struct F64Exact {
     const unsigned ex = expo(x);
     return within(c, 100) && (is_zero(x) || (ex - 63u <= 1920u && ex - expo(c) + 1000u <= 2000u));
   }
+  // c = +-2^k, normal: x / c is x * RN(1/c) exactly, so one rounding of the
+  // product is the quotient's, for every x (subnormal, zero and non-finite
+  // included).  c is the same for the whole launch, so is the branch.
+  static __device__ __forceinline__ bool pow2(T c) {
+    unsigned lo, hi;
+    halves(c, lo, hi);
+    return lo == 0u && (hi & 0xfffffu) == 0u && expo(c) - 1u <= 2045u;
+  }
   static __device__ __forceinline__ T divu(T x, T c, T rc, bool&) {
 #ifdef FGB_DIVU_IEEE
     (void)rc;
     return __ddiv_rn(x, c);
 #else
+    if (pow2(c)) return __dmul_rn(x, rc);
     if (warp_all(divu_window(x, c))) return markstein(x, c, rc);
     return __ddiv_rn(x, c);
 #endif
@@ -159,6 +168,7 @@ struct F64Exact {
     (void)rc;
     return __ddiv_rn(x, c);
 #endif
+    if (pow2(c)) return smul(x, rc);
     if (!warp_all(divu_window(x, c))) return __ddiv_rn(x, c);
     const T q = smul(x, rc);
     const T e = __fma_rn(-q, c, x);

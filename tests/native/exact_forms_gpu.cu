@@ -54,7 +54,9 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
     const uint64_t warp = i / 32;
     const int ca = (int)(mix(warp * 3 + seed) % 6), cb = (int)(mix(warp * 5 + seed) % 6);
     // divu: uniform divisor per warp (grid-independent), numerator per lane
-    const double c = operand(warp * 11 + seed, ca == 3 ? 1 : ca % 2);
+    double c = operand(warp * 11 + seed, ca == 3 ? 1 : ca % 2);
+    if ((warp & 3) == 3)   // powers of two, whose quotient is one product
+      c = __longlong_as_double((long long)(__double_as_longlong(c) & 0xfff0000000000000ull));
     const double rc = 1.0 / c;
     const double x = operand(key * 7 + 1, cb == 5 ? (int)(mix(key) % 6) : cb);
     bool ok = true;
