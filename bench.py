@@ -422,6 +422,8 @@ def run_ours(args, spec):
     # end to end through the drop-in C API: upload + spf steps + download per call
     for _ in range(2):
         dp.forward(1)
+    e2e_sampler = ClockSampler(local)
+    e2e_sampler.start()
     t0 = time.perf_counter()
     e2e_calls = max(1, min(args.steps, args.e2e_steps))
     for _ in range(e2e_calls):
@@ -429,7 +431,8 @@ def run_ours(args, spec):
     e2e_s = time.perf_counter() - t0
     e2e = {"value": ws * cells * e2e_calls * spf / e2e_s / 1e9, "unit": "GLUP/s",
            "h2d_bytes_per_step": nf * cells * 8, "d2h_bytes_per_step": nf * cells * 8,
-           "steps": e2e_calls, "api": "Formura_Forward (drop-in C API, formura_data on the host)"}
+           "steps": e2e_calls, "api": "Formura_Forward (drop-in C API, formura_data on the host)",
+           "clocks": e2e_sampler.stop()}
     launches_e2e = 0
 
     variants = {}
