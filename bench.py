@@ -99,8 +99,16 @@ class ClockSampler:
             for nm, v in zip(names, s[5:9]):
                 if v.strip().lower() == "active":
                     reasons.add(nm)
+        pw = []
+        for smp in self.samples:
+            try:
+                pw.append(float(smp[3]))
+            except (ValueError, IndexError):
+                pass
         return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_min_mhz": min(sm) if sm else None,
                 "sm_max_mhz": max(mx) if mx else None,
+                "power_w": statistics.median(pw) if pw else None,
                 "reasons": sorted(reasons), "samples": len(self.samples)}
 
 
