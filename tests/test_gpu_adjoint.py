@@ -204,3 +204,27 @@ def test_hllc_density_gradient_against_central_differences(prec, tol):
         fd = (loss(u0 + eps * v) - loss(u0 - eps * v)) / (2 * eps)
         ad = float(np.vdot(grad, v))
         assert abs(fd - ad) <= tol * abs(fd), (fd, ad)
+
+
+@pytest.mark.parametrize("program", ["hllc3d", "sod1d"])
+def test_f32_backward_matches_f64(program):
+    """The FP32 adjoint step gathers the linear update stage's partial sums
+    directly; the FP64 step stores and gathers them.  On the same state and
+    seed both give the same lambda up to FP32 rounding."""
+    rng = np.random.default_rng(6)
+    if program == "hllc3d":
+        g64, u = _hllc(16)
+        g32, _ = _hllc(16, "f32")
+    else:
+        src, cfg = builtin_program("sod1d")
+        _, U = program_uniforms(src, cfg, "sod1d")
+        g64, g32 = Grid("sod1d", (400,), "f64", U), Grid("sod1d", (400,), "f32", U)
+        r = rng.uniform(-1, 1, (3, 400))
+        u = np.stack([2.5 + 0.1 * r[0], 0.3 * r[1], 1 + 0.1 * r[2]])
+    w = rng.standard_normal(u.shape)
+    lam = []
+    for g in (g64, g32):
+        g.upload(u)
+        lam.append(g.backward(w))
+        g.close()
+    assert W.rel_l2(lam[1], lam[0]) < 1e-5, W.rel_l2(lam[1], lam[0])
