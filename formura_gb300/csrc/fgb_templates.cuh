@@ -71,6 +71,37 @@ struct F64Exact {
   // biased exponent field within [1023 - w, 1023 + w]
   static __device__ __forceinline__ bool within(T x, unsigned w) { return expo(x) - (1023u - w) <= 2u * w; }
 
+  // IEEE comparisons on the integer pipe (an FP64 compare costs the FP64
+  // pipe as much as an FMA): an order key per operand, its magnitude bits
+  // negated when the sign is set, so that -0 and +0 share the key 0; any
+  // comparison with a NaN is false, except !=.
+  static __device__ __forceinline__ long long okey(T x, bool& nan) {
+    unsigned lo, hi;
+    halves(x, lo, hi);
+    const unsigned mhi = hi & 0x7fffffffu;
+    nan = mhi > 0x7ff00000u || (mhi == 0x7ff00000u && lo != 0u);
+    const long long mag = (long long)(((unsigned long long)mhi << 32) | lo);
+    return (hi >> 31) ? -mag : mag;
+  }
+  static __device__ __forceinline__ bool lt(T a, T b) {
+    bool na, nb;
+    const long long ka = okey(a, na), kb = okey(b, nb);
+    return !(na || nb) && ka < kb;
+  }
+  static __device__ __forceinline__ bool gt(T a, T b) { return lt(b, a); }
+  static __device__ __forceinline__ bool le(T a, T b) {
+    bool na, nb;
+    const long long ka = okey(a, na), kb = okey(b, nb);
+    return !(na || nb) && ka <= kb;
+  }
+  static __device__ __forceinline__ bool ge(T a, T b) { return le(b, a); }
+  static __device__ __forceinline__ bool eq(T a, T b) {
+    bool na, nb;
+    const long long ka = okey(a, na), kb = okey(b, nb);
+    return !(na || nb) && ka == kb;
+  }
+  static __device__ __forceinline__ bool ne(T a, T b) { return !eq(a, b); }
+
   // a*h + t for a = +-2^k (a literal): one rounding of the exact sum, which
   // is the reference's RN(RN(a*h) + t) as long as a*h is exact, that is h
   // is zero or a*h stays normal.
@@ -192,6 +223,12 @@ struct F64Ieee {
   using Deriv = F64Fast;
   using Ieee = F64Ieee;
   static constexpr bool kChecked = false;
+  static __device__ __forceinline__ bool lt(T a, T b) { return a < b; }
+  static __device__ __forceinline__ bool gt(T a, T b) { return a > b; }
+  static __device__ __forceinline__ bool le(T a, T b) { return a <= b; }
+  static __device__ __forceinline__ bool ge(T a, T b) { return a >= b; }
+  static __device__ __forceinline__ bool eq(T a, T b) { return a == b; }
+  static __device__ __forceinline__ bool ne(T a, T b) { return a != b; }
   static __device__ __forceinline__ T add(T a, T b) { return __dadd_rn(a, b); }
   static __device__ __forceinline__ T sub(T a, T b) { return __dsub_rn(a, b); }
   static __device__ __forceinline__ T mul(T a, T b) { return __dmul_rn(a, b); }
@@ -222,6 +259,12 @@ struct F64Fast {
   using Deriv = F64Fast;
   using Ieee = F64Fast;
   static constexpr bool kChecked = false;
+  static __device__ __forceinline__ bool lt(T a, T b) { return a < b; }
+  static __device__ __forceinline__ bool gt(T a, T b) { return a > b; }
+  static __device__ __forceinline__ bool le(T a, T b) { return a <= b; }
+  static __device__ __forceinline__ bool ge(T a, T b) { return a >= b; }
+  static __device__ __forceinline__ bool eq(T a, T b) { return a == b; }
+  static __device__ __forceinline__ bool ne(T a, T b) { return a != b; }
   static __device__ __forceinline__ T add(T a, T b) { return a + b; }
   static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }
@@ -256,6 +299,12 @@ struct F32 {
   using Deriv = F32;
   using Ieee = F32;
   static constexpr bool kChecked = false;
+  static __device__ __forceinline__ bool lt(T a, T b) { return a < b; }
+  static __device__ __forceinline__ bool gt(T a, T b) { return a > b; }
+  static __device__ __forceinline__ bool le(T a, T b) { return a <= b; }
+  static __device__ __forceinline__ bool ge(T a, T b) { return a >= b; }
+  static __device__ __forceinline__ bool eq(T a, T b) { return a == b; }
+  static __device__ __forceinline__ bool ne(T a, T b) { return a != b; }
   static __device__ __forceinline__ T add(T a, T b) { return a + b; }
   static __device__ __forceinline__ T sub(T a, T b) { return a - b; }
   static __device__ __forceinline__ T mul(T a, T b) { return a * b; }

@@ -305,6 +305,9 @@ def build_stages(step: List[MMNode]) -> List[Stage]:
 # --------------------------------------------------------------------------
 _EXT = {"sqrt": "sqrt", "fabs": "fabs", "exp": "exp", "log": "log", "sin": "sin", "cos": "cos"}
 _CMP = {"<", ">", "<=", ">=", "==", "!="}
+# comparisons are policy calls: the bit-faithful FP64 policy evaluates them
+# on the integer pipe
+_CMP_NAME = {"<": "lt", ">": "gt", "<=": "le", ">=": "ge", "==": "eq", "!=": "ne"}
 
 # Operations with an integer-pipe form (the s-prefixed policy methods): the
 # FP64 pipe time of the hardware form in units of one add, and the part of
@@ -456,7 +459,7 @@ class _StageEmitter:
             a = self.operand(micro, inst[2])
             b = self.operand(micro, inst[3])
             if op in _CMP:
-                return self.bind(f"({self.as_T(a)} {op} {self.as_T(b)})", "bool")
+                return self.bind(f"{self.P}::{_CMP_NAME[op]}({self.as_T(a)}, {self.as_T(b)})", "bool")
             if op in ("&&", "||"):
                 return self.bind(f"({self.as_bool(a)} {op} {self.as_bool(b)})", "bool")
             if op == "*":

@@ -45,9 +45,10 @@ __device__ __forceinline__ bool same(double a, double b) {
 // A division must give the IEEE result's bits for every lane (it falls back
 // to the IEEE division by itself); the multiply-add wherever its range flag
 // stays set (where it drops, the kernels evaluate with F64Ieee instead).
-// Counts per operation: mismatches, and lanes inside the shortened window.
+// Counts per operation: mismatches, and lanes inside the shortened window;
+// then the mismatches of the integer-pipe comparisons.
 __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
-  unsigned long long bad[3] = {0, 0, 0}, fast[3] = {0, 0, 0};
+  unsigned long long bad[4] = {0, 0, 0, 0}, fast[3] = {0, 0, 0};
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
     const uint64_t key = seed * 0x100000000ull + i;
@@ -78,20 +79,29 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
     r = F64Exact::fma(f, h, t, ok);
     fast[2] += ok;
     bad[2] += ok && !same(r, __dadd_rn(__dmul_rn(f, h), t));
+    // comparisons on the integer pipe against the hardware's, every operand
+    // class against every other (signed zeros, infinities and NaNs included),
+    // and each value against itself and its negation
+    const double p = operand(key * 7 + 6, (int)(mix(key ^ 2) % 6)), q = (i & 8) ? -p : (i & 16) ? p : b;
+    const bool hw[6] = {p < q, p > q, p <= q, p >= q, p == q, p != q};
+    const bool in[6] = {F64Exact::lt(p, q), F64Exact::gt(p, q), F64Exact::le(p, q),
+                        F64Exact::ge(p, q), F64Exact::eq(p, q), F64Exact::ne(p, q)};
+    for (int j = 0; j < 6; ++j) bad[3] += hw[j] != in[j];
   }
   for (int j = 0; j < 3; ++j) {
     atomicAdd(&out[j], bad[j]);
     atomicAdd(&out[3 + j], fast[j]);
   }
+  atomicAdd(&out[6], bad[3]);
 }
 
 extern "C" int exact_forms_gpu_check(unsigned long long seed, unsigned long long n, unsigned long long* host_out) {
   unsigned long long* d = nullptr;
-  if (cudaMalloc(&d, 6 * sizeof(unsigned long long)) != cudaSuccess) return 1;
-  cudaMemset(d, 0, 6 * sizeof(unsigned long long));
+  if (cudaMalloc(&d, 7 * sizeof(unsigned long long)) != cudaSuccess) return 1;
+  cudaMemset(d, 0, 7 * sizeof(unsigned long long));
   check<<<152 * 8, 256>>>(seed, n, d);
   cudaError_t e = cudaDeviceSynchronize();
-  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 6 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 7 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
   cudaFree(d);
   return e == cudaSuccess ? 0 : 2;
 }

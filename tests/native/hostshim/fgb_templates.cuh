@@ -48,6 +48,12 @@ struct Exact {
   static T fma(T a, T b, T c, bool&) { return a * b + c; }
   static T divu(T x, T c, T, bool&) { return x / c; }
   static T rcp(T b) { return 1.0 / b; }
+  static bool lt(T a, T b) { return a < b; }
+  static bool gt(T a, T b) { return a > b; }
+  static bool le(T a, T b) { return a <= b; }
+  static bool ge(T a, T b) { return a >= b; }
+  static bool eq(T a, T b) { return a == b; }
+  static bool ne(T a, T b) { return a != b; }
   static T divr(T a, T b, T, bool&) { return a / b; }
   static T sadd(T a, T b) { return a + b; }
   static T ssub(T a, T b) { return a - b; }
