@@ -58,6 +58,11 @@ struct F64Exact {
   static __device__ __forceinline__ void halves(T x, unsigned& lo, unsigned& hi) {
     asm("mov.b64 {%0, %1}, %2;" : "=r"(lo), "=r"(hi) : "d"(x));
   }
+  static __device__ __forceinline__ T join(unsigned lo, unsigned hi) {
+    T r;
+    asm("mov.b64 %0, {%1, %2};" : "=d"(r) : "r"(lo), "r"(hi));
+    return r;
+  }
   static __device__ __forceinline__ unsigned expo(T x) {
     unsigned lo, hi;
     halves(x, lo, hi);
@@ -207,7 +212,12 @@ struct F64Exact {
   }
   static __device__ __forceinline__ T neg(T a) { return -a; }
   static __device__ __forceinline__ T sqrt(T a) { return __dsqrt_rn(a); }
-  static __device__ __forceinline__ T fabs(T a) { return ::fabs(a); }
+  // |a| by clearing the sign bit on the integer pipe (exact, NaN included)
+  static __device__ __forceinline__ T fabs(T a) {
+    unsigned lo, hi;
+    halves(a, lo, hi);
+    return join(lo, hi & 0x7fffffffu);
+  }
   static __device__ __forceinline__ T exp(T a) { return ::exp(a); }
   static __device__ __forceinline__ T log(T a) { return ::log(a); }
   static __device__ __forceinline__ T sin(T a) { return ::sin(a); }

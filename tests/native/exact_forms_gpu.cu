@@ -87,6 +87,7 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
     const bool in[6] = {F64Exact::lt(p, q), F64Exact::gt(p, q), F64Exact::le(p, q),
                         F64Exact::ge(p, q), F64Exact::eq(p, q), F64Exact::ne(p, q)};
     for (int j = 0; j < 6; ++j) bad[3] += hw[j] != in[j];
+    bad[3] += !same(F64Exact::fabs(p), fabs(p)) || (__double_as_longlong(F64Exact::fabs(p)) >> 63) != 0;
   }
   for (int j = 0; j < 3; ++j) {
     atomicAdd(&out[j], bad[j]);
