@@ -5,7 +5,9 @@
  * numerators) it need not, which is why the device falls back there.
  * The windows: for a grid-independent c in [2^-100, 2^100], numerators of
  * exponent in [-960, 960] whose quotient's exponent is in [-1000, 1000];
- * for a shared reciprocal, both operands in [2^-400, 2^400].
+ * for a shared reciprocal, both operands in [2^-400, 2^400]; and normal
+ * numerators below the first window, scaled by 2^256 into it, whose quotient
+ * (exponent at least -1000) is scaled back.
  * Uses the host's correctly rounded fma.  Prints "mismatches_inside outside". */
 #include <math.h>
 #include <stdint.h>
@@ -57,6 +59,17 @@ int main(int argc, char** argv) {
     r = corrected(x2, c2, 1.0 / c2);
     w = x2 / c2;
     inside += bits(r) != bits(w);
+    /* tiny normal numerators below the window whose quotient is normal:
+       scaled by 2^256 into the window and the quotient scaled back */
+    double c4 = mant_operand(1023 - 100, 1023 + 100, (int)(i % 3));
+    int e4 = (int)((bits(c4) >> 52) & 0x7ff) - 1023;
+    int lo4 = -1022 > e4 - 1000 ? -1022 : e4 - 1000;
+    if (lo4 <= -961) {
+      double x4 = mant_operand(1023 + lo4, 1023 - 961, (int)((i / 3) % 3));
+      r = ldexp(corrected(ldexp(x4, 256), c4, 1.0 / c4), -256);
+      w = x4 / c4;
+      inside += bits(r) != bits(w);
+    }
     /* the quotient's lowest exponents: large constants, small numerators */
     double c3 = mant_operand(1023 + 90, 1023 + 100, (int)(i % 3));
     int e3 = (int)((bits(c3) >> 52) & 0x7ff) - 1023;
