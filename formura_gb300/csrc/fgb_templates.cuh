@@ -150,24 +150,12 @@ struct F64Exact {
     return __ddiv_rn(x, c);
 #else
     if (pow2(c)) return __dmul_rn(x, rc);
-    const bool in = divu_window(x, c);
-    if (warp_all(in)) return markstein(x, c, rc);
-    // normal numerators below the window whose quotient is normal (a field
-    // decaying towards zero): scaled by 2^256 into the window, the corrected
-    // quotient scaled back, both exactly; two products more than in-window
-    const bool scaled = divu_scaled(x, c);
-    if (warp_all(in || scaled)) {
-      const T q = markstein(__dmul_rn(x, scaled ? 0x1p256 : 1.0), c, rc);
-      return __dmul_rn(q, scaled ? 0x1p-256 : 1.0);
-    }
+    if (warp_all(divu_window(x, c))) return markstein(x, c, rc);
+    // (Scaling normal numerators below the window by 2^256 into it, with the
+    // quotient scaled back, is exact too, but as a third path it slowed the
+    // common one: Gray-Scott FP64 13.8 against 15.1 GLUP/s.)
     return __ddiv_rn(x, c);
 #endif
-  }
-  // x normal below the window (exponent under -960), quotient exponent at
-  // least -1000, c in [2^-100, 2^100]
-  static __device__ __forceinline__ bool divu_scaled(T x, T c) {
-    const unsigned ex = expo(x);
-    return within(c, 100) && ex - 1u < 62u && ex + 1000u >= expo(c);
   }
   // RN(1/b) for a grid value b that several quotients divide by
   static __device__ __forceinline__ T rcp(T b) { return __drcp_rn(b); }
