@@ -9,6 +9,7 @@
 #define FGB_MAX_MIDS 160
 #define FGB_MAX_STAGES 8
 #define FGB_NUM_PRECISIONS 4
+#define FGB_MAX_DIVISORS 64
 
 // Arguments of one stage launch.  Field and intermediate pointers are
 // device pointers; their element type is fixed by the precision (storage
@@ -108,6 +109,12 @@ struct FgbProgramDesc {
   int adj_pairs[FGB_MAX_STAGES];
   int adj_parts[FGB_MAX_STAGES];   // partial-sum kernels per stage
   int adj_recompute[FGB_MAX_STAGES];   // forward arrays of the stage read by the partial sums
+  // Uniform-table slots of the grid-independent divisors; when all of them
+  // are powers of two for a grid, its FP64 steps use launch_p2, whose
+  // division by them is one product.
+  int ndivisors;
+  int divisors[FGB_MAX_DIVISORS];
+  FgbStageLaunch launch_p2[FGB_MAX_STAGES];
 };
 
 typedef const FgbProgramDesc* (*FgbProgramGetter)(void);

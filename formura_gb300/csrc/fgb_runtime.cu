@@ -99,9 +99,19 @@ __global__ void field_partial_sums(const S* __restrict__ a, size_t n, double* __
 
 }  // namespace
 
+// a normal power of two (+-2^k): division by it is exact as one product
+// with its reciprocal, which is then a power of two as well
+static bool is_pow2(double c) {
+  uint64_t u;
+  memcpy(&u, &c, sizeof u);
+  const unsigned e = (unsigned)(u >> 52) & 0x7ffu;
+  return (u & 0x000fffffffffffffull) == 0 && e >= 1u && e <= 2046u;
+}
+
 struct fgb_grid {
   const FgbProgramDesc* prog = nullptr;
   int precision = 0;
+  bool p2 = false;   // FP64 steps through launch_p2 (every divisor a power of two)
   int n[3] = {1, 1, 1};
   size_t cells = 0;
   cudaStream_t stream = nullptr;
@@ -224,7 +234,7 @@ static int run_steps(fgb_grid* g, int nsteps) {
   }
   for (int s = 0; s < nsteps; ++s) {
     for (int st = 0; st < g->prog->nstages; ++st) {
-      cudaError_t e = g->prog->launch[g->precision][st](&L[g->cur], g->stream);
+      cudaError_t e = (g->p2 ? g->prog->launch_p2[st] : g->prog->launch[g->precision][st])(&L[g->cur], g->stream);
       if (e != cudaSuccess) return cuda_fail(e, "stage launch");
       ++g->launches;
     }
@@ -302,6 +312,10 @@ int fgb_open(const char* program, const int* shape, int ndim, int precision, con
   if (e == cudaSuccess && d->nmids > 0) e = cudaMalloc(&g->mids, cells * d->nmids * cs);
   if (e == cudaSuccess && d->nuniforms > 0) e = cudaMalloc(&g->uniforms, d->nuniforms * cs);
   if (e == cudaSuccess && precision >= FGB_F32) e = cudaMalloc((void**)&g->staging, cells * d->nfields * 8);
+  if (precision == FGB_F64 && d->ndivisors > 0) {
+    g->p2 = true;
+    for (int i = 0; i < d->ndivisors; ++i) g->p2 = g->p2 && is_pow2(uniforms[d->divisors[i]]);
+  }
   if (e == cudaSuccess && d->nuniforms > 0) {
     if (cs == 8) {
       e = cudaMemcpy(g->uniforms, uniforms, d->nuniforms * 8, cudaMemcpyHostToDevice);

@@ -487,6 +487,11 @@ class _StageEmitter:
                     if b[0] == "lit" and is_pow2(b[1]):
                         return self.bind(f"{self.P}::mul({self.as_T(a)}, T({c_double(1.0 / b[1])}))")
                     rc = self.recip_handle(dep)
+                    if self.P == "M" and self.p.divisor_slots is not None:
+                        if b[0] == "u":
+                            self.p.divisor_slots.add(self.p.table_index(b[1]))
+                        else:
+                            self.p.divisor_slots = None
                     return self.bind(f"{self.P}::divu({self.as_T(a)}, {self.as_T(b)}, {self.as_T(rc)}, fgb_ok)")
                 if self.reciprocal:
                     r = self.bind(f"{self.P}::div(T(1), {self.as_T(b)})")
@@ -579,6 +584,9 @@ class _ProgramEmitter:
         self.soft_cost = soft_cost_default()
         self.stage_adjoint = stage_adjoint
         self.adjoint_pairs: List[List[tuple]] = []
+        # uniform-table slots the forward divides by (M::divu); None once a
+        # divisor is a literal that is not a power of two
+        self.divisor_slots: Optional[Set[int]] = set()
         rng = calc_range(self.mmg)
         s = self.sleeve
         stores = [n for n in self.mmg if n.is_store]
@@ -645,6 +653,9 @@ class _ProgramEmitter:
             out.append(adj_src)
         if stage_adj:
             out.append(stage_adj)
+        div_slots = sorted(self.divisor_slots) if self.divisor_slots is not None else []
+        div_count = len(div_slots) if self.divisor_slots is not None else -1
+        div_list = ", ".join(str(i) for i in div_slots) if div_slots else "0"
         out.append(f"struct Prog {{\n"
                    f"  using Adjoint = {'AdjointStep' if adj_src else 'void'};\n"
                    f"  using StageAdjoint = {'StageAdjointList' if stage_adj else 'void'};\n"
@@ -656,6 +667,9 @@ class _ProgramEmitter:
                    f"  static constexpr int kShift = {self.shift};\n"
                    f"  static constexpr int kReach = {self.reach};\n"
                    f"  static constexpr int kUniforms = {len(self.table)};\n"
+                   f"  // uniform-table slots of the divisors (-1: a literal divisor)\n"
+                   f"  static constexpr int kNumDivisors = {div_count};\n"
+                   f"  static constexpr int kDivisors[{max(1, len(div_slots))}] = {{{div_list}}};\n"
                    f"}};\n")
         out += stage_texts
         out.append(f"}}  // namespace fgb_gen_{self.name}\n")

@@ -61,6 +61,9 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
     const double rc = 1.0 / c;
     const double x = operand(key * 7 + 1, cb == 5 ? (int)(mix(key) % 6) : cb);
     bool ok = true;
+    if ((warp & 3) == 3) {   // the power-of-two policy's single product, for every numerator
+      if (!same(fgb::F64ExactP2::divu(x, c, rc, ok), __ddiv_rn(x, c))) ++bad[0];
+    }
     double r = F64Exact::divu(x, c, rc, ok);
     fast[0] += F64Exact::divu_window(x, c);
     bad[0] += ok && !same(r, __ddiv_rn(x, c));
