@@ -142,11 +142,28 @@ struct F64Exact {
     return __ddiv_rn(x, c);
 #else
     if (warp_all(divu_window(x, c))) return markstein(x, c, rc);
-    // (Scaling normal numerators below the window by 2^256 into it, with the
-    // quotient scaled back, is exact too, but as a third path it slowed the
-    // common one: Gray-Scott FP64 13.8 against 15.1 GLUP/s.)
-    return __ddiv_rn(x, c);
+    return divu_outside(x, c, rc);
 #endif
+  }
+  // x normal below the window (exponent under -960), quotient exponent at
+  // least -1000, c in [2^-100, 2^100]
+  static __device__ __forceinline__ bool divu_scaled(T x, T c) {
+    const unsigned ex = expo(x);
+    return within(c, 100) && ex - 1u < 62u && ex + 1000u >= expo(c);
+  }
+  // A warp with a numerator outside the window (a field decaying through
+  // tiny values).  Normal numerators below the window whose quotient is
+  // normal are scaled by 2^256 into it and the quotient scaled back, both
+  // exactly, for five FP64 instructions instead of the IEEE division's ten;
+  // the rest take the IEEE division.  Out of line, so that the compiler
+  // cannot fold its extra products into the common path.
+  static __device__ __noinline__ T divu_outside(T x, T c, T rc) {
+    const bool scaled = divu_scaled(x, c);
+    if (warp_all(divu_window(x, c) || scaled)) {
+      const T q = markstein(__dmul_rn(x, scaled ? 0x1p256 : 1.0), c, rc);
+      return __dmul_rn(q, scaled ? 0x1p-256 : 1.0);
+    }
+    return __ddiv_rn(x, c);
   }
   // RN(1/b) for a grid value b that several quotients divide by
   static __device__ __forceinline__ T rcp(T b) { return __drcp_rn(b); }
