@@ -210,3 +210,48 @@ def test_reference_program_through_cuda_emitter(tmp_path, name):
         u = host.forward(u)
     for i, f in enumerate(ref.fields):
         assert np.array_equal(u[i], ref.get(f)), f
+
+
+# ---------------------------------------------------------------------------
+# the divisor list that selects the power-of-two kernels of a grid
+# ---------------------------------------------------------------------------
+_DIV_PROGRAM = """dimension :: 1
+axes :: x
+
+begin function q = init()
+  double [] :: q = 0
+end function
+
+begin function q_new = step(q)
+  q_new = q + (q[i+1] + q[i-1]) / dx{extra}
+end function
+"""
+
+
+@pytest.mark.parametrize("extra,count", [("", 1), (" + (q[i+1] - q[i-1]) / 4.0", 1),
+                                         (" + (q[i+1] - q[i-1]) / 3.0", -1)])
+def test_divisor_slots_for_the_power_of_two_kernels(extra, count):
+    """A grid steps with the kernels whose division by a constant is one
+    product only if every divisor is a power of two.  The generator lists the
+    uniform-table slots the host checks; a literal divisor that is a power of
+    two needs no slot (it is a product already), and one that is not makes
+    the program ineligible (-1)."""
+    import re
+    from formura_gb300.generator.config import decode_config
+    from formura_gb300.generator.cuda import emit_cuda
+    from formura_gb300.generator.manifest import compile_program
+    cfg = "length_per_node: [1.0]\ngrid_per_node: [16]\nwith_omp: 1\n"
+    kp = emit_cuda(compile_program(_DIV_PROGRAM.format(extra=extra), decode_config(cfg)), "divtest", [],
+                   stage_adjoint=False)
+    assert re.findall(r"kNumDivisors = (-?\d+)", kp.source) == [str(count)]
+
+
+def test_shipped_programs_divisor_slots(generated):
+    """heat3d, gs2d and hllc3d divide by their grid spacings only (table
+    slots), so grids whose spacing is a power of two take the single-product
+    kernels."""
+    import re
+    for program, n in (("heat3d", 3), ("gs2d", 4), ("hllc3d", 3)):
+        with open(generated[program]) as f:
+            src = f.read()
+        assert re.findall(r"kNumDivisors = (-?\d+)", src)[0] == str(n), program
