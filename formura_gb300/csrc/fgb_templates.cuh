@@ -40,12 +40,13 @@ struct F64Exact {
   using Ieee = F64Ieee;
   static constexpr bool kChecked = true;
   // Arithmetic of the generated adjoint kernels: contracted FP64.  The
-  // arrays an adjoint step recomputes for later stages keep this exact
-  // policy, but the forward values a partial-sum kernel differentiates and
-  // its derivative terms are contracted, and a quotient there is a product
-  // with the reciprocal that the derivative needs anyway.  A gradient is
-  // checked against finite differences and the dot-product identity, not bit
-  // patterns; a fused multiply-add is one FP64 instruction instead of two.
+  // forward steps of a gradient keep this exact policy, but the arrays an
+  // adjoint step recomputes (with the F64Fast stage kernels), the forward
+  // values a partial-sum kernel differentiates and its derivative terms are
+  // contracted, and a quotient there is a product with the reciprocal that
+  // the derivative needs anyway.  A gradient is checked against finite
+  // differences and the dot-product identity, not bit patterns; a fused
+  // multiply-add is one FP64 instruction instead of two.
   using Deriv = F64Fast;
   static __device__ __forceinline__ T add(T a, T b) { return __dadd_rn(a, b); }
   static __device__ __forceinline__ T sub(T a, T b) { return __dsub_rn(a, b); }
