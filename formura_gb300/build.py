@@ -21,6 +21,7 @@ ROOT = os.path.dirname(HERE)
 GEN = os.path.join(HERE, "_gen")
 BUILD = os.path.join(HERE, "_build")
 LIB = os.path.join(BUILD, "libformura_gb300.so")
+PROBE_LIB = os.path.join(BUILD, "libfgb_probe.so")   # FP64 pipe throughput probe
 PROGRAMS = os.path.join(HERE, "programs")
 CSRC = os.path.join(HERE, "csrc")
 
@@ -134,7 +135,7 @@ def build(names: Optional[List[str]] = None, jobs: Optional[int] = None, verbose
         raise RuntimeError("nvcc not found: the CUDA toolkit is required to build formura_gb300")
     gen = generate(names)
     os.makedirs(BUILD, exist_ok=True)
-    deps = [os.path.join(CSRC, f) for f in ("fgb_internal.h", "fgb_templates.cuh", "fgb_fused.cuh", "fgb_softf64.h")
+    deps = [os.path.join(CSRC, f) for f in ("fgb_internal.h", "fgb_templates.cuh", "fgb_fused.cuh")
             if os.path.exists(os.path.join(CSRC, f))] + [os.path.join(ROOT, "include", "formura_gb300.h")]
     units = [(os.path.join(CSRC, "fgb_runtime.cu"), os.path.join(BUILD, "fgb_runtime.o")),
              (os.path.join(CSRC, "fgb_noalloc.cu"), os.path.join(BUILD, "fgb_noalloc.o")),
@@ -151,6 +152,13 @@ def build(names: Optional[List[str]] = None, jobs: Optional[int] = None, verbose
     if r.returncode != 0:
         raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + r.stderr[-4000:])
     os.replace(tmp, LIB)
+    probe_obj = _compile(os.path.join(CSRC, "fgb_probe.cu"), os.path.join(BUILD, "fgb_probe.o"), [])
+    tmp = PROBE_LIB + f".tmp{os.getpid()}"
+    cmd = ["nvcc", *ARCH, "-shared", "-o", tmp, probe_obj, "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + r.stderr[-4000:])
+    os.replace(tmp, PROBE_LIB)
     if verbose:
         print("built", LIB)
     return LIB

@@ -45,6 +45,31 @@ int error(int code, const char* fmt, ...) {
 
 size_t align256(size_t x) { return (x + 255) & ~(size_t)255; }
 
+// a normal power of two: division by it is one exact product, so FP64 steps
+// may use the program's launch_p2 kernels (the choice fgb_open makes)
+bool is_pow2(double c) {
+  uint64_t u;
+  memcpy(&u, &c, sizeof u);
+  const unsigned e = (unsigned)(u >> 52) & 0x7ffu;
+  return (u & 0x000fffffffffffffull) == 0 && e >= 1u && e <= 2046u;
+}
+
+// The uniform table travels as a kernel parameter (copied at launch), so no
+// host buffer has to outlive the call and no pageable copy is queued.
+struct UniformTable {
+  double v[FGB_NOALLOC_MAX_UNIFORMS];
+};
+static_assert(sizeof(UniformTable) <= 16384, "uniform table exceeds the kernel parameter space used here");
+
+__global__ void write_uniforms(UniformTable t, int n, int as_float, void* dst) {
+  for (int i = threadIdx.x; i < n; i += blockDim.x) {
+    if (as_float)
+      static_cast<float*>(dst)[i] = (float)t.v[i];
+    else
+      static_cast<double*>(dst)[i] = t.v[i];
+  }
+}
+
 // The device address of the scratch array on the current device.  In host
 // code `fgb_noalloc_scratch` is only a host-side stand-in for the symbol, so
 // the address is looked up once per device with that device current.
@@ -91,6 +116,9 @@ extern "C" int fgb_forward_noalloc(const char* program, const int* shape, int nd
     n[3 - ndim + a] = shape[a];
     cells *= (size_t)shape[a];
   }
+  // the stage kernels index fields and cells with 32-bit integers
+  if (cells * (size_t)d->nfields >= ((size_t)1 << 32) || cells >= ((size_t)1 << 31))
+    return error(FGB_E_ARG, "grid of %zu points is larger than this build supports", cells);
   const size_t es = precision <= FGB_F64_FAST ? 8 : (precision == FGB_F32 ? 4 : 2);
   const size_t cs = precision <= FGB_F64_FAST ? 8 : 4;
   const size_t state_bytes = cells * d->nfields * es;
@@ -118,14 +146,16 @@ extern "C" int fgb_forward_noalloc(const char* program, const int* shape, int nd
     return e == cudaSuccess ? FGB_OK : error(FGB_E_CUDA, "copy: %s", cudaGetErrorString(e));
   }
   if (nuniforms > 0) {
-    if (cs == 8) {
-      e = cudaMemcpyAsync(scratch, uniforms, nuniforms * 8, cudaMemcpyHostToDevice, st);
-    } else {
-      float u32[FGB_NOALLOC_MAX_UNIFORMS];
-      for (int i = 0; i < nuniforms; ++i) u32[i] = (float)uniforms[i];
-      e = cudaMemcpyAsync(scratch, u32, nuniforms * 4, cudaMemcpyHostToDevice, st);
-    }
+    UniformTable t;
+    memcpy(t.v, uniforms, (size_t)nuniforms * sizeof(double));
+    write_uniforms<<<1, 128, 0, st>>>(t, nuniforms, cs == 4, scratch);
+    e = cudaGetLastError();
     if (e != cudaSuccess) return error(FGB_E_CUDA, "uniform table: %s", cudaGetErrorString(e));
+  }
+  bool p2 = false;
+  if (precision == FGB_F64 && d->ndivisors > 0) {
+    p2 = true;
+    for (int i = 0; i < d->ndivisors; ++i) p2 = p2 && is_pow2(uniforms[d->divisors[i]]);
   }
   void* bufs[2] = {out_state, scratch + off_state};
   FgbLaunch L;
@@ -147,7 +177,7 @@ extern "C" int fgb_forward_noalloc(const char* program, const int* shape, int nd
       L.out[f] = static_cast<char*>(dst) + f * cells * es;
     }
     for (int stg = 0; stg < d->nstages; ++stg) {
-      e = d->launch[precision][stg](&L, st);
+      e = (p2 ? d->launch_p2[stg] : d->launch[precision][stg])(&L, st);
       if (e != cudaSuccess) return error(FGB_E_CUDA, "stage launch: %s", cudaGetErrorString(e));
     }
     src = dst;

@@ -9,7 +9,6 @@
 #include <stdint.h>
 #include <type_traits>
 #include "fgb_internal.h"
-#include "fgb_softf64.h"
 
 namespace fgb {
 
@@ -176,51 +175,6 @@ struct F64Exact {
     if (warp_all(divr_window(a, b))) return markstein(a, b, y);
     return __ddiv_rn(a, b);
   }
-  // The same operations on the integer pipes (fgb_softf64.h), with the
-  // hardware instruction for the operands outside the fast path: the
-  // generated code sends part of its adds, multiplies and power-of-two
-  // multiply-adds here so that both pipes work.  Bit-identical results.
-  // The hardware fallback sits behind a warp-uniform branch: a predicated
-  // FP64 instruction would still take its turn on the FP64 pipe.
-  static __device__ __forceinline__ T sadd(T a, T b) {
-    uint64_t r;
-    const bool ok = soft::add_bits(soft::to_bits(a), soft::to_bits(b), r);
-    T v = soft::from_bits(r);
-    if (__any_sync(__activemask(), !ok)) v = ok ? v : __dadd_rn(a, b);
-    return v;
-  }
-  static __device__ __forceinline__ T ssub(T a, T b) {
-    uint64_t r;
-    const bool ok = soft::add_bits(soft::to_bits(a), soft::to_bits(b) ^ soft::kSign, r);
-    T v = soft::from_bits(r);
-    if (__any_sync(__activemask(), !ok)) v = ok ? v : __dsub_rn(a, b);
-    return v;
-  }
-  static __device__ __forceinline__ T smul(T a, T b) {
-    uint64_t r;
-    const bool ok = soft::mul_bits(soft::to_bits(a), soft::to_bits(b), r);
-    T v = soft::from_bits(r);
-    if (__any_sync(__activemask(), !ok)) v = ok ? v : __dmul_rn(a, b);
-    return v;
-  }
-  static __device__ __forceinline__ T sfma(T c, T h, T t, bool& ok) {
-    uint64_t r;
-    const bool fast = soft::scaled_add_bits(soft::to_bits(c), soft::to_bits(h), soft::to_bits(t), r);
-    T v = soft::from_bits(r);
-    if (__any_sync(__activemask(), !fast)) v = fast ? v : fma(c, h, t, ok);
-    return v;
-  }
-  // Markstein quotient with its first product on the integer pipes
-  static __device__ __forceinline__ T sdivu(T x, T c, T rc, bool&) {
-#ifdef FGB_DIVU_IEEE
-    (void)rc;
-    return __ddiv_rn(x, c);
-#endif
-    if (!warp_all(divu_window(x, c))) return __ddiv_rn(x, c);
-    const T q = smul(x, rc);
-    const T e = __fma_rn(-q, c, x);
-    return is_zero(x) ? q : __fma_rn(e, rc, q);
-  }
   static __device__ __forceinline__ T neg(T a) { return -a; }
   static __device__ __forceinline__ T sqrt(T a) { return __dsqrt_rn(a); }
   // |a| by clearing the sign bit on the integer pipe (exact, NaN included)
@@ -258,11 +212,6 @@ struct F64Ieee {
   static __device__ __forceinline__ T divu(T x, T c, T, bool&) { return __ddiv_rn(x, c); }
   static __device__ __forceinline__ T rcp(T b) { return __drcp_rn(b); }
   static __device__ __forceinline__ T divr(T a, T b, T, bool&) { return __ddiv_rn(a, b); }
-  static __device__ __forceinline__ T sadd(T a, T b) { return __dadd_rn(a, b); }
-  static __device__ __forceinline__ T ssub(T a, T b) { return __dsub_rn(a, b); }
-  static __device__ __forceinline__ T smul(T a, T b) { return __dmul_rn(a, b); }
-  static __device__ __forceinline__ T sfma(T a, T h, T t, bool& ok) { return fma(a, h, t, ok); }
-  static __device__ __forceinline__ T sdivu(T x, T c, T rc, bool& ok) { return divu(x, c, rc, ok); }
   static __device__ __forceinline__ T neg(T a) { return -a; }
   static __device__ __forceinline__ T sqrt(T a) { return __dsqrt_rn(a); }
   static __device__ __forceinline__ T fabs(T a) { return ::fabs(a); }
@@ -281,7 +230,6 @@ struct F64Ieee {
 // a power of two, 11 % (16.0 -> 14.3 GLUP/s).
 struct F64ExactP2 : F64Exact {
   static __device__ __forceinline__ T divu(T x, T, T rc, bool&) { return __dmul_rn(x, rc); }
-  static __device__ __forceinline__ T sdivu(T x, T, T rc, bool&) { return smul(x, rc); }
 };
 
 // FP64 with contraction and reciprocal multiplication (not bit-faithful).
@@ -305,11 +253,6 @@ struct F64Fast {
   static __device__ __forceinline__ T divu(T x, T, T rc, bool&) { return x * rc; }
   static __device__ __forceinline__ T rcp(T b) { return __drcp_rn(b); }
   static __device__ __forceinline__ T divr(T a, T, T y, bool&) { return a * y; }
-  static __device__ __forceinline__ T sadd(T a, T b) { return a + b; }
-  static __device__ __forceinline__ T ssub(T a, T b) { return a - b; }
-  static __device__ __forceinline__ T smul(T a, T b) { return a * b; }
-  static __device__ __forceinline__ T sfma(T a, T b, T c, bool&) { return ::fma(a, b, c); }
-  static __device__ __forceinline__ T sdivu(T x, T, T rc, bool&) { return x * rc; }
   static __device__ __forceinline__ T neg(T a) { return -a; }
   static __device__ __forceinline__ T sqrt(T a) { return ::sqrt(a); }
   static __device__ __forceinline__ T fabs(T a) { return ::fabs(a); }
@@ -347,11 +290,6 @@ struct F32 {
   static __device__ __forceinline__ T divu(T x, T, T rc, bool&) { return x * rc; }
   static __device__ __forceinline__ T rcp(T b) { return __fdividef(1.0f, b); }
   static __device__ __forceinline__ T divr(T a, T, T y, bool&) { return a * y; }
-  static __device__ __forceinline__ T sadd(T a, T b) { return a + b; }
-  static __device__ __forceinline__ T ssub(T a, T b) { return a - b; }
-  static __device__ __forceinline__ T smul(T a, T b) { return a * b; }
-  static __device__ __forceinline__ T sfma(T a, T b, T c, bool&) { return fmaf(a, b, c); }
-  static __device__ __forceinline__ T sdivu(T x, T, T rc, bool&) { return x * rc; }
   static __device__ __forceinline__ T neg(T a) { return -a; }
   static __device__ __forceinline__ T sqrt(T a) { return sqrtf(a); }
   static __device__ __forceinline__ T fabs(T a) { return fabsf(a); }

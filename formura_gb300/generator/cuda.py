@@ -309,30 +309,6 @@ _CMP = {"<", ">", "<=", ">=", "==", "!="}
 # on the integer pipe
 _CMP_NAME = {"<": "lt", ">": "gt", "<=": "le", ">=": "ge", "==": "eq", "!=": "ne"}
 
-# Operations with an integer-pipe form (the s-prefixed policy methods): the
-# FP64 pipe time of the hardware form in units of one add, and the part of
-# it that stays on the FP64 pipe in the integer-pipe form.
-_SOFT_FORMS = {"M::add(": ("M::sadd(", 1.0, 0.0), "M::sub(": ("M::ssub(", 1.0, 0.0),
-               "M::mul(": ("M::smul(", 1.0, 0.0), "M::fma(": ("M::sfma(", 1.0, 0.0),
-               "M::divu(": ("M::sdivu(", 3.0, 2.0)}
-# FP64 pipe time of operations without one (division and square root take
-# about ten times an add on this part)
-_HW_ONLY = {"M::div(": 10.0, "M::sqrt(": 10.0}
-
-
-def soft_cost_default() -> Optional[float]:
-    """Issue time of one integer-pipe operation in units of one FP64-pipe
-    add, from FGB_SOFT_COST; unset or 'off' keeps every operation on the FP64
-    pipe.  Off by default: measured on GB300, the integer forms cost about 80
-    instructions each, and the 64-bit integer multiplies of the product form
-    issue to the FP64 pipe themselves, so Gray-Scott FP64 ran at 0.53-0.78x
-    of the all-FP64-pipe kernel for every cost tried (0.5, 0.7, 1.0)."""
-    v = os.environ.get("FGB_SOFT_COST", "off").strip().lower()
-    if v in ("off", "none", "inf", ""):
-        return None
-    return float(v)
-
-
 class _StageEmitter:
     """Emits one stage's SSA chain.  ``policy`` names the arithmetic policy
     of the operations (``M``, the kernel's, or ``D``, its derivative policy);
@@ -355,8 +331,6 @@ class _StageEmitter:
         self.var: Dict[tuple, object] = {}     # key -> expression handle
         self.memo: Dict[tuple, tuple] = {}     # (expression, type) -> handle
         self.n = 0
-        self.load_fp64 = 0.0                   # balance of the two pipes
-        self.load_int = 0.0
         self.scaled: Dict[tuple, str] = {}     # materialised power-of-two products
 
     def fresh(self) -> str:
@@ -522,26 +496,6 @@ class _StageEmitter:
             return "true" if h[1] != 0.0 else "false"
         return f"({self.as_T(h)} != T(0))"
 
-    def pipe(self, expr: str) -> str:
-        """Send the operation to the FP64 pipe or to its integer-pipe form,
-        whichever keeps the two pipes' accumulated time more even."""
-        for hw, cost in _HW_ONLY.items():
-            if expr.startswith(hw):
-                self.load_fp64 += cost
-                return expr
-        for hw, (sw, hw_cost, kept) in _SOFT_FORMS.items():
-            if not expr.startswith(hw):
-                continue
-            c = self.p.soft_cost
-            if c is not None and max(self.load_fp64 + kept, self.load_int + c) <= \
-                    max(self.load_fp64 + hw_cost, self.load_int):
-                self.load_int += c
-                self.load_fp64 += kept
-                return sw + expr[len(hw):]
-            self.load_fp64 += hw_cost
-            return expr
-        return expr
-
     def bind(self, expr: str, ctype: str = "T", prefix: Optional[str] = None):
         # value numbering: the same operation on the same operands is the same
         # value (every operation is deterministic), so it is computed once.
@@ -555,7 +509,7 @@ class _StageEmitter:
         else:
             self.nr += 1
             name = f"{prefix}{self.nr}"
-        self.emit(f"const {ctype} {name} = {self.pipe(expr)};")
+        self.emit(f"const {ctype} {name} = {expr};")
         h = ("v", name, ctype)
         self.memo[(expr, ctype)] = h
         return h
@@ -581,7 +535,6 @@ class _ProgramEmitter:
         self.stages = build_stages(self.mmg)
         self.mids = sorted({m for s in self.stages for m in s.mid_out})
         self.table: List[tuple] = []
-        self.soft_cost = soft_cost_default()
         self.stage_adjoint = stage_adjoint
         self.adjoint_pairs: List[List[tuple]] = []
         # uniform-table slots the forward divides by (M::divu); None once a

@@ -41,6 +41,11 @@ sys.path.insert(0, os.path.dirname(os.path.dirname(os.path.abspath(__file__))))
 from formura_gb300.generator.manifest import MMProgram, MMNode, calc_range  # noqa: E402
 
 
+# A kernel whose manifest temporaries add up to more than this keeps them on
+# the heap (see mk_kernel).
+HEAP_TEMPORARY_BYTES = 512 << 20
+
+
 # --------------------------------------------------------------------------
 # printing helpers
 # --------------------------------------------------------------------------
@@ -172,11 +177,22 @@ class Emitter:
         rng = calc_range(mmg)
         lines = []
         tmps = [n for n in mmg if not n.is_store]
+        total = sum(math.prod(s - rng[n.omid].size() for s in in_size) * 8 for n in tmps)
         for n in tmps:
             if n.om_type[0] != "gridtype":
                 raise ValueError("manifest scalar values are not supported by the reference emitter")
             ds = rng[n.omid].size()
-            lines.append(f"static double formura_mn{n.omid}{idx_str(str(s - ds) for s in in_size)};")
+            dims = [s - ds for s in in_size]
+            if total <= HEAP_TEMPORARY_BYTES:
+                lines.append(f"static double formura_mn{n.omid}{idx_str(map(str, dims))};")
+            else:
+                # Same array, same indexing, allocated once on first use: a
+                # static array this large cannot be addressed from code in a
+                # shared object (x86-64 and aarch64 reach +-2 / 4 GB of
+                # PC-relative data), and aarch64 has no medium code model.
+                v = f"formura_mn{n.omid}"
+                lines.append(f"static double (*{v}){idx_str(map(str, dims[1:]))} = 0;")
+                lines.append(f"if (!{v}) {{ {v} = calloc({dims[0]}, sizeof *{v}); if (!{v}) abort(); }}")
         for n in mmg:
             r = rng[n.omid]
             size = [s - r.size() for s in in_size]

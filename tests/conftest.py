@@ -5,7 +5,9 @@ ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
 if ROOT not in sys.path:
     sys.path.insert(0, ROOT)
 
-REFERENCE = "/root/reference"
+# Checkout of the reference (formura/formura): read as text by the CPU tests
+# that compile its programs and drivers; those tests skip without it.
+REFERENCE = os.environ.get("FORMURA_REFERENCE", "/root/reference")
 
 
 def pytest_configure(config):

@@ -28,7 +28,7 @@ sys.path.insert(0, ROOT)
 from formura_gb300 import workloads as W  # noqa: E402
 from oracle.reference_lib import ReferenceProgram  # noqa: E402
 
-REF = "/root/reference"
+REF = os.environ.get("FORMURA_REFERENCE", "/root/reference")
 OUT = os.path.dirname(os.path.abspath(__file__))
 
 

@@ -55,11 +55,6 @@ struct Exact {
   static bool eq(T a, T b) { return a == b; }
   static bool ne(T a, T b) { return a != b; }
   static T divr(T a, T b, T, bool&) { return a / b; }
-  static T sadd(T a, T b) { return a + b; }
-  static T ssub(T a, T b) { return a - b; }
-  static T smul(T a, T b) { return a * b; }
-  static T sfma(T a, T b, T c, bool&) { return a * b + c; }
-  static T sdivu(T x, T c, T, bool&) { return x / c; }
   static T neg(T a) { return -a; }
   static T sqrt(T a) { return std::sqrt(a); }
   static T fabs(T a) { return std::fabs(a); }

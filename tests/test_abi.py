@@ -50,3 +50,22 @@ def test_open_errors_are_reported_not_fatal(lib):
     assert rc == -1 and b"dimensional" in lib.fgb_last_error()
     rc = lib.fgb_open(b"gs2d", shape, 2, 9, None, 0, ctypes.byref(h))
     assert rc == -1
+
+
+def test_noalloc_rejects_grids_beyond_32bit_indexing(lib):
+    """fgb_forward_noalloc applies fgb_open's size limit before it touches
+    any pointer or the device: 1300^3 points exceed the 2^31 cells that the
+    stage kernels' 32-bit indices cover, even though one step of heat3d
+    would need scratch only for its uniform table."""
+    lib.fgb_last_error.restype = ctypes.c_char_p
+    fn = lib.fgb_forward_noalloc
+    fn.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int,
+                   ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_void_p, ctypes.c_void_p,
+                   ctypes.c_int, ctypes.c_void_p]
+    nu = ctypes.c_int()
+    assert lib.fgb_program_query(b"heat3d", None, None, ctypes.byref(nu), None, None) == 0
+    u = (ctypes.c_double * max(1, nu.value))(*([0.1] * max(1, nu.value)))
+    shape = (ctypes.c_int * 3)(1300, 1300, 1300)
+    # fake, never dereferenced device addresses far apart
+    rc = fn(b"heat3d", shape, 3, 0, u, nu.value, ctypes.c_void_p(1 << 40), ctypes.c_void_p(1 << 44), 1, None)
+    assert rc == -1 and b"larger than this build supports" in lib.fgb_last_error()

@@ -20,7 +20,7 @@ from formura_gb300 import workloads as W
 from formura_gb300.host import builtin_program
 from oracle.reference_lib import ReferenceProgram
 
-REF = "/root/reference"
+from conftest import REFERENCE as REF
 GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
 
 

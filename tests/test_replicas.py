@@ -48,7 +48,7 @@ def test_reference_arm_runs_on_rank_zero_only(monkeypatch):
     spec = bench.workload_spec("gs2d")
 
     class Args:
-        warmup, steps = 1, 1
+        warmup, steps, spf = 1, 1, 1000
 
     buf = io.StringIO()
     with redirect_stdout(buf):
@@ -65,7 +65,7 @@ def test_reference_arm_line_on_a_small_grid(monkeypatch):
     spec.update(cfg=W.gs_config(64), shape=(64, 64), cpu_tb=[(4, 36)])
 
     class Args:
-        warmup, steps = 1, 3
+        warmup, steps, spf = 1, 3, 8
 
     buf = io.StringIO()
     with redirect_stdout(buf):
@@ -76,7 +76,9 @@ def test_reference_arm_line_on_a_small_grid(monkeypatch):
     assert line["e2e"]["h2d_bytes_per_step"] == 0
     assert sorted(line["config"]["probed_configs_GLUPs"]) == ["NoBlocking",
                                                               "TemporalBlocking nt=4 grid_per_block=36"]
-    assert line["config"]["time_steps_per_bench_step"] in (1, 4)
+    # a bench step is spf time steps on both arms, whichever blocking wins
+    assert line["config"]["time_steps_per_bench_step"] == 8
+    assert line["config"]["timed_time_steps"].startswith("0..24")
 
 
 @pytest.mark.parametrize("name", ["gs2d", "heat3d", "hllc3d", "hlld3d"])

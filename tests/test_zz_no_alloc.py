@@ -23,6 +23,7 @@ pytestmark = pytest.mark.gpu
 
 def _noalloc(lib, program, shape, precision, U, d_in, d_out, nsteps, stream):
     L = lib.lib
+    L.fgb_last_error.restype = ctypes.c_char_p
     L.fgb_forward_noalloc.argtypes = [ctypes.c_char_p, ctypes.POINTER(ctypes.c_int), ctypes.c_int, ctypes.c_int,
                                       ctypes.POINTER(ctypes.c_double), ctypes.c_int, ctypes.c_void_p,
                                       ctypes.c_void_p, ctypes.c_int, ctypes.c_void_p]
@@ -71,9 +72,12 @@ def test_noalloc_matches_allocating_path(program, shape, prec, steps):
     g.close()
 
     # two calls in a row: a -> b, then b -> a
+    a_before = d_a.clone()
     rc = _noalloc(lib, program, shape, pnum, U, d_a.data_ptr(), d_b.data_ptr(), steps[0], s)
     assert rc == 0, lib.lib.fgb_last_error()
     torch.cuda.synchronize()
+    # the input state is left as it was
+    assert torch.equal(d_a, a_before)
     got1 = d_b.cpu().numpy().astype(np.float64)
     rc = _noalloc(lib, program, shape, pnum, U, d_b.data_ptr(), d_a.data_ptr(), steps[1], s)
     assert rc == 0, lib.lib.fgb_last_error()
