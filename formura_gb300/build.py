@@ -11,6 +11,7 @@ import concurrent.futures as cf
 import hashlib
 import json
 import os
+import re
 import shutil
 import subprocess
 import sys
@@ -61,16 +62,20 @@ def library_runtime_params(name: str) -> List[str]:
     return runtime_params(program_sources(name)[1])
 
 
-def generate(names: Optional[List[str]] = None) -> Dict[str, str]:
-    """Emit device code for each program; return name -> .cu path."""
+def generate(names: Optional[List[str]] = None, sources: Optional[Dict[str, tuple]] = None,
+             gen_dir: str = GEN) -> Dict[str, str]:
+    """Emit device code for each program and the registry of the library;
+    return name -> .cu path.  Programs are the shipped ones (`names`, default
+    all) or, with `sources`, name -> (.fmr text, .yaml text)."""
     from .generator.config import decode_config
     from .generator.cuda import emit_cuda
     from .generator.manifest import compile_program
-    os.makedirs(GEN, exist_ok=True)
+    os.makedirs(gen_dir, exist_ok=True)
     out = {}
     registered: List[str] = []
-    for name in names or program_names():
-        src, cfg = program_sources(name)
+    if sources is None:
+        sources = {name: program_sources(name) for name in (names or program_names())}
+    for name, (src, cfg) in sources.items():
         mm = compile_program(src, decode_config(cfg))
         kp = emit_cuda(mm, name, runtime_params(cfg))
         text = kp.source
@@ -80,21 +85,21 @@ def generate(names: Optional[List[str]] = None) -> Dict[str, str]:
                 sub = emit_cuda(mm, name, runtime_params(cfg), graph)
                 text += "\n" + sub.source
                 subs.append(f"{name}__{graph}")
-        path = os.path.join(GEN, f"prog_{name}.cu")
+        path = os.path.join(gen_dir, f"prog_{name}.cu")
         _write_if_changed(path, text)
         meta = {"name": name, "fields": kp.fields, "dim": kp.dim, "sleeve": kp.sleeve,
                 "shift": kp.shift, "nuniforms": len(kp.uniform_exprs),
                 "stages": len(kp.stages), "mids": len(kp.mids), "subprograms": subs}
-        _write_if_changed(os.path.join(GEN, f"prog_{name}.json"), json.dumps(meta, indent=1) + "\n")
+        _write_if_changed(os.path.join(gen_dir, f"prog_{name}.json"), json.dumps(meta, indent=1) + "\n")
         out[name] = path
         registered.extend([name] + subs)
-    reg = ['#include "../csrc/fgb_internal.h"']
+    reg = ['#include "fgb_internal.h"']
     names = sorted(registered)
     reg += [f'extern "C" const FgbProgramDesc* fgb_program_{n}(void);' for n in names]
     reg.append('extern "C" const FgbProgramGetter fgb_builtin_programs[] = {'
                + ", ".join(f"&fgb_program_{n}" for n in names) + "};")
     reg.append(f'extern "C" const int fgb_builtin_program_count = {len(names)};')
-    _write_if_changed(os.path.join(GEN, "fgb_registry.cu"), "\n".join(reg) + "\n")
+    _write_if_changed(os.path.join(gen_dir, "fgb_registry.cu"), "\n".join(reg) + "\n")
     return out
 
 
@@ -129,36 +134,72 @@ def _compile(src: str, obj: str, deps: List[str]) -> str:
     return obj
 
 
+RUNTIME_UNITS = ("fgb_runtime", "fgb_noalloc", "fgb_batch", "fgb_lazy")
+
+
+def _deps() -> List[str]:
+    return [os.path.join(CSRC, f) for f in ("fgb_internal.h", "fgb_templates.cuh", "fgb_fused.cuh", "fgb_wait.cuh")
+            if os.path.exists(os.path.join(CSRC, f))] + [os.path.join(ROOT, "include", "formura_gb300.h")]
+
+
+def _link(objs: List[str], out: str):
+    tmp = out + f".tmp{os.getpid()}"
+    cmd = ["nvcc", *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
+    r = subprocess.run(cmd, capture_output=True, text=True)
+    if r.returncode != 0:
+        raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + r.stderr[-4000:])
+    os.replace(tmp, out)
+
+
+def _library(gen: Dict[str, str], gen_dir: str, obj_dir: str, out: str, jobs: Optional[int]):
+    """Compile the runtime (program-independent objects, cached in the
+    library's build folder), the programs and their registry; link `out`."""
+    os.makedirs(BUILD, exist_ok=True)
+    os.makedirs(obj_dir, exist_ok=True)
+    deps = _deps()
+    units = [(os.path.join(CSRC, u + ".cu"), os.path.join(BUILD, u + ".o")) for u in RUNTIME_UNITS]
+    units.append((os.path.join(gen_dir, "fgb_registry.cu"), os.path.join(obj_dir, "fgb_registry.o")))
+    units += [(p, os.path.join(obj_dir, f"prog_{n}.o")) for n, p in gen.items()]
+    jobs = jobs or max(2, min(len(units), os.cpu_count() or 4))
+    with cf.ThreadPoolExecutor(jobs) as ex:
+        objs = list(ex.map(lambda u: _compile(u[0], u[1], deps), units))
+    _link(objs, out)
+
+
+def program_identifier(name: str) -> str:
+    """A library program name usable in C identifiers (the generated kernels
+    live in namespace fgb_gen_<name>): '3d_hllc' becomes 'p3d_hllc'."""
+    ident = re.sub(r"\W", "_", name)
+    return "p" + ident if not ident or ident[0].isdigit() else ident
+
+
+def build_program_library(name: str, fmr_src: str, yaml_text: str, out: str,
+                          jobs: Optional[int] = None, verbose: bool = False) -> str:
+    """A library like libformura_gb300.so whose kernels are those of one
+    user program (a .fmr with its numerical config), registered under
+    `name`: the counterpart of running the reference's `formura` on a new
+    program.  The generated C body (generator/cli.py) opens the program by
+    that name.  Returns the library path."""
+    if shutil.which("nvcc") is None:
+        raise RuntimeError("nvcc not found: the CUDA toolkit is required to build formura_gb300")
+    if program_identifier(name) != name:
+        raise ValueError(f"program name {name!r} is not a C identifier; use {program_identifier(name)!r}")
+    key = hashlib.sha1((name + "\0" + fmr_src + "\0" + yaml_text).encode()).hexdigest()[:12]
+    gen_dir = os.path.join(BUILD, "user", f"{name}_{key}")
+    gen = generate(sources={name: (fmr_src, yaml_text)}, gen_dir=gen_dir)
+    _library(gen, gen_dir, gen_dir, out, jobs)
+    if verbose:
+        print("built", out)
+    return out
+
+
 def build(names: Optional[List[str]] = None, jobs: Optional[int] = None, verbose: bool = False) -> str:
     """Generate, compile and link; returns the library path."""
     if shutil.which("nvcc") is None:
         raise RuntimeError("nvcc not found: the CUDA toolkit is required to build formura_gb300")
     gen = generate(names)
-    os.makedirs(BUILD, exist_ok=True)
-    deps = [os.path.join(CSRC, f) for f in ("fgb_internal.h", "fgb_templates.cuh", "fgb_fused.cuh")
-            if os.path.exists(os.path.join(CSRC, f))] + [os.path.join(ROOT, "include", "formura_gb300.h")]
-    units = [(os.path.join(CSRC, "fgb_runtime.cu"), os.path.join(BUILD, "fgb_runtime.o")),
-             (os.path.join(CSRC, "fgb_noalloc.cu"), os.path.join(BUILD, "fgb_noalloc.o")),
-             (os.path.join(CSRC, "fgb_batch.cu"), os.path.join(BUILD, "fgb_batch.o")),
-             (os.path.join(CSRC, "fgb_lazy.cu"), os.path.join(BUILD, "fgb_lazy.o")),
-             (os.path.join(GEN, "fgb_registry.cu"), os.path.join(BUILD, "fgb_registry.o"))]
-    units += [(p, os.path.join(BUILD, f"prog_{n}.o")) for n, p in gen.items()]
-    jobs = jobs or max(2, min(len(units), os.cpu_count() or 4))
-    with cf.ThreadPoolExecutor(jobs) as ex:
-        objs = list(ex.map(lambda u: _compile(u[0], u[1], deps), units))
-    tmp = LIB + f".tmp{os.getpid()}"
-    cmd = ["nvcc", *ARCH, "-shared", "-o", tmp, *objs, "-lcudart"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + r.stderr[-4000:])
-    os.replace(tmp, LIB)
-    probe_obj = _compile(os.path.join(CSRC, "fgb_probe.cu"), os.path.join(BUILD, "fgb_probe.o"), [])
-    tmp = PROBE_LIB + f".tmp{os.getpid()}"
-    cmd = ["nvcc", *ARCH, "-shared", "-o", tmp, probe_obj, "-lcudart"]
-    r = subprocess.run(cmd, capture_output=True, text=True)
-    if r.returncode != 0:
-        raise RuntimeError("link failed:\n" + " ".join(cmd) + "\n" + r.stderr[-4000:])
-    os.replace(tmp, PROBE_LIB)
+    _library(gen, GEN, BUILD, LIB, jobs)
+    _link([_compile(os.path.join(CSRC, "fgb_probe.cu"), os.path.join(BUILD, "fgb_probe.o"), [])], PROBE_LIB)
     if verbose:
         print("built", LIB)
     return LIB

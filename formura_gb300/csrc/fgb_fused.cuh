@@ -9,6 +9,7 @@
 // to K single steps of the generic kernel.
 #pragma once
 #include "fgb_templates.cuh"
+#include "fgb_wait.cuh"
 
 namespace fgb {
 
@@ -61,26 +62,13 @@ __device__ __forceinline__ int pwrap(int a, int n) {
   return a >= n ? a - n : a;
 }
 
-// Polls an mbarrier phase at most 2^20 times; true once the phase with the
-// given parity has completed.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-  uint32_t done = 0;
-  for (int it = 0; it < (1 << 20) && !done; ++it)
-    asm volatile(
-        "{\n .reg .pred p;\n mbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n selp.u32 %0, 1, 0, p;\n}"
-        : "=r"(done)
-        : "r"(bar), "r"(parity)
-        : "memory");
-  return done != 0;
-}
-
 // TMA load of one tile (with halo) per field into shared memory: one
 // elected thread arms an mbarrier with the expected bytes and issues one 2D
-// box copy per field; every thread waits on the barrier with a bounded
-// number of polls.  Returns false (and raises the launch's error flag) if the
-// wait ran out; the leader then waits once more, also bounded, so that a late
-// copy lands before the block's shared memory is released.  The box lies
-// inside the grid: the caller checks that.
+// box copy per field; every thread waits on the barrier for at most one
+// second of the global timer.  Returns false (and raises the launch's error
+// flag) if the wait ran out; the leader then waits once more, with the
+// longer drain limit, so that a late copy lands before the block's shared
+// memory is released.  The box lies inside the grid: the caller checks that.
 template <class T, int NF, int PLANE>
 __device__ __forceinline__ bool tma_load_tile(const FgbLaunch& L, T* smem, int x, int y) {
   __shared__ __align__(8) uint64_t bar;
@@ -107,7 +95,7 @@ __device__ __forceinline__ bool tma_load_tile(const FgbLaunch& L, T* smem, int x
   }
   const bool ok = __syncthreads_and(mbar_wait_bounded(b, 0u));
   if (!ok && leader) {
-    mbar_wait_bounded(b, 0u);
+    mbar_wait_bounded(b, 0u, kDrainLimitNs);
     if (L.err) atomicExch(L.err, 1);
   }
   return ok;
@@ -510,7 +498,7 @@ __global__ void __launch_bounds__(BX * BY) tb3d_kernel(const __grid_constant__ F
             // shared memory is released
             for (int z = zin; z <= zin + D && z < zend; ++z)
               mbar_wait_bounded((uint32_t)__cvta_generic_to_shared(&bars[ring_slot(z, P0)]),
-                                (uint32_t)((z - zfirst) / P0) & 1u);
+                                (uint32_t)((z - zfirst) / P0) & 1u, kDrainLimitNs);
             if (L.err) atomicExch(L.err, 2);
           }
           return;

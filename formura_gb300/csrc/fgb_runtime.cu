@@ -208,6 +208,11 @@ static void make_tensor_maps(fgb_grid* g) {
   g->tmaps = dev;
 }
 
+// Device address of a grid's error word (not part of the public header):
+// lets a test raise the word from its own kernel, whose bounded wait runs out
+// on a barrier nothing completes, and check how the runtime reports it.
+extern "C" int* fgb_internal_error_word(fgb_grid* g) { return g ? g->err : nullptr; }
+
 // a kernel's bounded wait ran out: report it once and clear the flag
 static int check_device_flag(fgb_grid* g) {
   if (!g->err) return FGB_OK;

@@ -10,6 +10,14 @@ the ``.fmr`` file's name with ``.yaml`` (the reference's default name is
 ``X.yaml`` too).  ``--program`` names the library program whose kernels the
 body uses (default: the file's base name).  ``-v`` prints the manifest
 structure: sleeve, stages, manifest nodes.
+
+``--lib`` also builds ``lib<program>_gb300.so`` beside the C file: the
+GB300 library with this program's kernels (``build_program_library``), for
+programs that are not shipped with the package.  The program name is then
+the file's base name made into a C identifier (``3d_hllc`` becomes
+``p3d_hllc``).  A driver links it like the reference's generated C::
+
+    gcc main.c X.c -L<dir> -l<program>_gb300 -Wl,-rpath,<dir> -lm
 """
 from __future__ import annotations
 
@@ -32,6 +40,8 @@ def main(argv: Optional[List[str]] = None) -> int:
     ap.add_argument("-o", "--output", help="output C file (default: <source>.c)")
     ap.add_argument("--nc", help="numerical config YAML (default: <source>.yaml)")
     ap.add_argument("--program", help="library program providing the kernels (default: source base name)")
+    ap.add_argument("--lib", action="store_true",
+                    help="also build lib<program>_gb300.so with this program's kernels")
     ap.add_argument("-v", "--verbose", action="store_true")
     args = ap.parse_args(argv)
 
@@ -39,16 +49,23 @@ def main(argv: Optional[List[str]] = None) -> int:
     cpath = args.output or base + ".c"
     hpath = os.path.splitext(cpath)[0] + ".h"
     ncpath = args.nc or base + ".yaml"
-    program = args.program or os.path.basename(base)
+    from .. import build as B
+    program = args.program or (B.program_identifier(os.path.basename(base)) if args.lib
+                               else os.path.basename(base))
     try:
         nc = read_config(ncpath)
         with open(args.source) as f:
-            prog = parse_program(f.read(), nc)
+            fmr_src = f.read()
+        with open(ncpath) as f:
+            yaml_text = f.read()
+        prog = parse_program(fmr_src, nc)
         om = gen_om_program(prog)
         mm = gen_mm_program(om)
-        from .. import build as B
-        rp = B.library_runtime_params(program) if os.path.exists(
-            os.path.join(B.PROGRAMS, program + ".yaml")) else []
+        if args.lib:
+            rp = B.runtime_params(yaml_text)
+        else:
+            rp = B.library_runtime_params(program) if os.path.exists(
+                os.path.join(B.PROGRAMS, program + ".yaml")) else []
         if args.verbose:
             kp = emit_cuda(mm, program, rp)
             rng = calc_range(mm.step)
@@ -71,6 +88,14 @@ def main(argv: Optional[List[str]] = None) -> int:
     print("Generate:")
     print("  " + cpath)
     print("  " + hpath)
+    if args.lib:
+        out = os.path.join(os.path.dirname(os.path.abspath(cpath)), f"lib{program}_gb300.so")
+        try:
+            B.build_program_library(program, fmr_src, yaml_text, out)
+        except (RuntimeError, ValueError, FormuraCompileError) as e:
+            print(f"formura-gb300: {e}", file=sys.stderr)
+            return 1
+        print("  " + out)
     return 0
 
 

@@ -183,3 +183,108 @@ def test_sod_shock_tube_oracle_matches_exact_solution():
         err_sample = np.mean(np.abs(d["sample_" + name][ss] - np.interp(xs[ss], d["exact_x"], d["exact_" + name])))
         assert err < 0.01 and err <= 1.01 * err_sample + 1e-12, (name, err, err_sample)
 
+
+
+def _physical(ref, field):
+    """A field of formura_data in physical order: index i holds position
+    (i + offset) mod N (Templates.hs:221-225, 346)."""
+    nav = ref.navi_dict()
+    a = ref.get(field)
+    return np.roll(a, tuple(nav[f"offset_{ax}"] for ax in "xyz"), (0, 1, 2))
+
+
+def _euler_case(ref, names, length, c_cfl, steps, seed):
+    """Steps the oracle and the numpy restatement of 3d_hllc.fmr from the
+    same smooth state; returns the largest relative max-norm difference and
+    whether every field agrees bit for bit."""
+    import numpy_euler as NE
+    ref.init()
+    shape = ref.shape
+    st = W.hllc_state(shape, seed=seed)
+    rho, m, e = st["rho"], (st["mx"], st["my"], st["mz"]), st["e"]
+    for name, val in zip(names, (rho, m[0], m[1], m[2], e)):
+        ref.set(name, val)
+    ref.forward(steps)
+    E = NE.Euler3D(shape, length, c_cfl=c_cfl)
+    for _ in range(steps):
+        rho, m, e = E.step(rho, m, e)
+    worst, exact = 0.0, True
+    for name, val in zip(names, (rho, m[0], m[1], m[2], e)):
+        got = _physical(ref, name)
+        worst = max(worst, float(np.abs(got - val).max() / np.abs(val).max()))
+        exact = exact and np.array_equal(got, val)
+    return worst, exact
+
+
+def test_hllc_oracle_equals_numpy_restatement():
+    """The shipped hllc3d program through the oracle against the numpy
+    restatement of the reference's 3d_hllc.fmr (no shared front end):
+    5 steps at 12^3 from the smooth Mach-0.3 state, CFL 0.4."""
+    n = 12
+    src, _ = builtin_program("hllc3d")
+    ref = ReferenceProgram(src, W.hllc_config(n), "hllc_np")
+    worst, exact = _euler_case(ref, ("rho", "mx", "my", "mz", "e"), (1.0, 1.0, 1.0), 0.4, 5, 3)
+    assert exact, f"largest relative difference {worst}"
+
+
+def test_reference_3d_hllc_oracle_equals_numpy_restatement():
+    """The reference's own 3d_hllc.fmr (its CFL 0.8 and box) through the
+    oracle, against the same numpy restatement: 4 steps at 12 x 12 x 12."""
+    path = os.path.join(REF, "sample", "3d_hllc", "3d_hllc.fmr")
+    if not os.path.exists(path):
+        pytest.skip("the reference tree is not present")
+    with open(path) as f:
+        src = f.read()
+    cfg = "length_per_node: [0.1, 0.5, 0.1]\ngrid_per_node: [12, 12, 12]\n"
+    ref = ReferenceProgram(src, cfg, "ref3dhllc_np")
+    worst, exact = _euler_case(ref, ("rho", "rhou", "rhov", "rhow", "e"), (0.1, 0.5, 0.1), 0.8, 4, 5)
+    assert exact, f"largest relative difference {worst}"
+
+
+def _mhd_case(ref, names, length, steps, seed):
+    """As _euler_case, for the HLLD program (9 fields, psi seeded too)."""
+    import numpy_mhd as NM
+    ref.init()
+    shape = ref.shape
+    st = W.mhd_state(shape, seed=seed)
+    st["psi"] = 0.01 * np.random.default_rng(seed + 1).standard_normal(shape)
+    comps = [st[k] for k in ("rho", "mx", "my", "mz", "bx", "by", "bz", "e", "psi")]
+    for name, val in zip(names, comps):
+        ref.set(name, val)
+    ref.forward(steps)
+    M = NM.MHD3D(shape, length)
+    for _ in range(steps):
+        comps = M.step(comps)
+    worst, exact = 0.0, True
+    for name, val in zip(names, comps):
+        got = _physical(ref, name)
+        worst = max(worst, float(np.abs(got - val).max() / np.abs(val).max()))
+        exact = exact and np.array_equal(got, val)
+    return worst, exact
+
+
+def test_hlld_oracle_equals_numpy_restatement():
+    """The shipped hlld3d program through the oracle against the numpy
+    restatement of the reference's mhd_3d_hlld.fmr: 3 steps at 10^3."""
+    n = 10
+    src, _ = builtin_program("hlld3d")
+    ref = ReferenceProgram(src, W.mhd_config(n), "hlld_np")
+    worst, exact = _mhd_case(ref, ("rho", "mx", "my", "mz", "bx", "by", "bz", "e", "psi"),
+                             (1.0, 1.0, 1.0), 3, 2)
+    assert exact, f"largest relative difference {worst}"
+
+
+def test_reference_mhd_3d_hlld_oracle_equals_numpy_restatement():
+    """The reference's own mhd_3d_hlld.fmr through the oracle, against the
+    same numpy restatement: 3 steps at 10 x 10 x 6 of its box."""
+    path = os.path.join(REF, "sample", "mhd_3d_hlld", "mhd_3d_hlld.fmr")
+    if not os.path.exists(path):
+        pytest.skip("the reference tree is not present")
+    with open(path) as f:
+        src = f.read()
+    length = (3.141592653589793, 3.141592653589793, 0.15707963267948966)
+    cfg = f"length_per_node: [{length[0]}, {length[1]}, {length[2]}]\ngrid_per_node: [10, 10, 6]\n"
+    ref = ReferenceProgram(src, cfg, "refmhd_np")
+    worst, exact = _mhd_case(ref, ("rho", "rhou", "rhov", "rhow", "B_x", "B_y", "B_z", "e", "psi"),
+                             length, 3, 4)
+    assert exact, f"largest relative difference {worst}"
