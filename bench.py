@@ -706,8 +706,9 @@ def run_adjoint(args):
                      "gradient_adjoint_steps": st["adjoint_steps"], "grad": grad,
                      "loss": 0.5 * float(np.vdot(uT - target, uT - target))}
         g.close()
-    # central differences in FP64
-    fd_grid = Grid("heat3d", shape, "f64fast", U)
+    # central differences of the bit-faithful FP64 forward, which equals the
+    # oracle (the reference generator's C) bit for bit
+    fd_grid = Grid("heat3d", shape, "f64", U)
 
     def loss(u):
         fd_grid.upload(u)

@@ -7,6 +7,7 @@ import pytest
 
 from formura_gb300 import workloads as W
 from formura_gb300.host import Grid, builtin_program, program_uniforms
+from oracle.reference_lib import ReferenceProgram
 
 pytestmark = pytest.mark.gpu
 
@@ -228,3 +229,65 @@ def test_f32_backward_matches_f64(program):
         lam.append(g.backward(w))
         g.close()
     assert W.rel_l2(lam[1], lam[0]) < 1e-4, W.rel_l2(lam[1], lam[0])
+
+
+# ---------------------------------------------------------------------------
+# reference gradients by differencing the oracle (the reference generator's
+# C, run on the host), as the finite-difference check of the adjoint
+# ---------------------------------------------------------------------------
+def _oracle_loss(program, cfg, fields, nsteps, target, tag):
+    """J(u) = 0.5 ||u_T - target||^2 with u_T from the oracle: Formura_Init,
+    u written into formura_data, nsteps Formura_Forward calls."""
+    src, _ = builtin_program(program)
+    ref = ReferenceProgram(src, cfg, f"{program}_fd_{tag}")
+
+    def loss(u):
+        ref.init()
+        for i, f in enumerate(fields):
+            ref.set(f, u[i])
+        ref.forward(nsteps)
+        d = np.stack([ref.get(f) for f in fields]) - target
+        return 0.5 * float(np.vdot(d, d))
+    return loss
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", 1e-6), ("f32", 2e-2)])
+def test_heat_gradient_against_oracle_differences(prec, tol):
+    """dJ/du_0 of the diffusion rollout (32^3, 50 steps, 8 checkpoints)
+    against central differences (eps 1e-6) of the oracle's loss on random
+    directions."""
+    n, nsteps = 32, 50
+    g, shape = _grid("heat3d", n, prec)
+    u0 = W.gaussians_3d(shape, 7, count=8)[None]
+    target = W.gaussians_3d(shape, 8, count=8)[None]
+    _, grad = g.gradient(u0, nsteps, 8, lambda uT: uT - target)
+    loss = _oracle_loss("heat3d", W.heat_config(n), ["q"], nsteps, target, "heat")
+    rng = np.random.default_rng(19)
+    eps = 1e-6
+    for _ in range(6):
+        v = rng.standard_normal(u0.shape)
+        fd = (loss(u0 + eps * v) - loss(u0 - eps * v)) / (2 * eps)
+        ad = float(np.vdot(grad, v))
+        assert abs(fd - ad) <= tol * abs(fd), (fd, ad)
+
+
+@pytest.mark.parametrize("prec,tol", [("f64", 2e-3), ("f32", 3e-2)])
+def test_hllc_density_gradient_against_oracle_differences(prec, tol):
+    """dJ/d rho_0 of the Euler rollout (16^3, 20 steps, the smooth Mach-0.3
+    state) against central differences (eps 1e-7) of the oracle's loss on
+    random density directions; the limiter's kinks bound the agreement as in
+    the GPU-forward check above."""
+    n, nsteps = 16, 20
+    g, u0 = _hllc(n, prec, seed=2)
+    target = u0 + 0.01 * np.random.default_rng(6).standard_normal(u0.shape)
+    _, grad = g.gradient(u0, nsteps, 4, lambda uT: uT - target)
+    loss = _oracle_loss("hllc3d", W.hllc_config(n), HLLC_FIELDS, nsteps, target, "hllc")
+    rng = np.random.default_rng(17)
+    eps = 1e-7
+    ir = HLLC_FIELDS.index("rho")
+    for _ in range(4):
+        v = np.zeros_like(u0)
+        v[ir] = rng.standard_normal(u0.shape[1:])
+        fd = (loss(u0 + eps * v) - loss(u0 - eps * v)) / (2 * eps)
+        ad = float(np.vdot(grad, v))
+        assert abs(fd - ad) <= tol * abs(fd), (fd, ad)
