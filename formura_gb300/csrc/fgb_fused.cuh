@@ -8,6 +8,9 @@
 // same generated stage functor runs per cell, so the result is bit-identical
 // to K single steps of the generic kernel.
 #pragma once
+#include <string.h>
+#include <utility>
+
 #include "fgb_templates.cuh"
 #include "fgb_wait.cuh"
 
@@ -235,6 +238,7 @@ struct Tb2dVariant {
   }
   static FgbFusedVariant describe() {
     FgbFusedVariant v;
+    v.x_multiple = 1;
     v.launch = &launch;
     v.tile_x = TX;
     v.tile_y = TY;
@@ -600,11 +604,183 @@ struct Tb3dVariant {
   }
   static FgbFusedVariant describe() {
     FgbFusedVariant v;
+    v.x_multiple = 1;
     v.launch = &launch;
     v.tile_x = TX;
     v.tile_y = TY;
     v.steps = K;
     v.smem_bytes = kSmem;
+    return v;
+  }
+};
+
+
+// ---------------------------------------------------------------------------
+// One step of a 3D single-stage program on rows of four-point vectors
+// ---------------------------------------------------------------------------
+// For programs whose stencil is a star of reach 1 (every load moves along at
+// most one axis, by at most one point) and whose step rolls the state by one
+// point (heat-like programs), in FP32 or FP16 storage.  A warp covers 128
+// consecutive points of a row.  A lane owns the four rolled destinations
+// x0..x0+3 (x0 a multiple of four) and stores them with one vector store;
+// their sources are x0-1..x0+2, whose x-neighbours are x0-2..x0+3: one
+// aligned vector load of x0..x0+3 and the last two values of the lane on the
+// left (warp shuffles; lane 0 loads those two itself).  The rows y-1 and y+1
+// and the planes z-1 and z+1 arrive the same way, so a thread issues about
+// one vector load per point it updates instead of seven scalar loads, and
+// every value the stage functor reads comes from registers.  Results are
+// those of the generic stage kernel, bit for bit.
+
+// four consecutive storage elements: one aligned vector load or store
+template <class S> struct Quad;
+template <> struct Quad<float> {
+  static __device__ __forceinline__ void get(const float* p, float, float v[4]) {
+    const float4 q = __ldg(reinterpret_cast<const float4*>(p));
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+    v[3] = q.w;
+  }
+  static __device__ __forceinline__ void put(float* p, const float v[4], float) {
+    *reinterpret_cast<float4*>(p) = make_float4(v[0], v[1], v[2], v[3]);
+  }
+};
+template <> struct Quad<__half> {
+  static __device__ __forceinline__ void get(const __half* p, float scale, float v[4]) {
+    const uint2 q = __ldg(reinterpret_cast<const uint2*>(p));
+    __half h[4];
+    memcpy(h, &q, sizeof q);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = Storage<__half, float>::load(h[i], scale);
+  }
+  static __device__ __forceinline__ void put(__half* p, const float v[4], float inv_scale) {
+    __half h[4];
+#pragma unroll
+    for (int i = 0; i < 4; ++i) h[i] = Storage<__half, float>::store(v[i], inv_scale);
+    uint2 q;
+    memcpy(&q, h, sizeof q);
+    *reinterpret_cast<uint2*>(p) = q;
+  }
+};
+
+// Accessor of one point (row R of the thread, element E of its four): the
+// centre plane's rows y-1 .. y+RY hold x0-2 .. x0+3, the planes z-1 and z+1
+// the thread's own rows.  Every index is a compile-time constant.
+template <class T, int NF, int RY, int R, int E>
+struct QuadAccess {
+  const T (&c)[NF][RY + 2][6];
+  const T (&z)[NF][2][RY][4];
+  T (&out)[NF][RY][4];
+  template <int F, int D0, int D1, int D2>
+  __device__ __forceinline__ T ld() const {
+    static_assert((D0 != 0) + (D1 != 0) + (D2 != 0) <= 1, "star stencils only");
+    static_assert(D0 >= -1 && D0 <= 1 && D1 >= -1 && D1 <= 1 && D2 >= -1 && D2 <= 1, "reach 1 only");
+    if constexpr (D0 == 0)
+      return c[F][R + 1 + D1][E + 1 + D2];
+    else
+      return z[F][D0 > 0 ? 1 : 0][R][E];
+  }
+  template <int F>
+  __device__ __forceinline__ void st(T v) const {
+    out[F][R][E] = v;
+  }
+};
+
+template <int... I, class Fn>
+__device__ __forceinline__ void static_for(std::integer_sequence<int, I...>, Fn&& fn) {
+  (fn(std::integral_constant<int, I>{}), ...);
+}
+
+template <class M, class S, class Stage, int NF, int RY, int BW>
+__global__ void __launch_bounds__(32 * BW) quad3d_kernel(const __grid_constant__ FgbLaunch L) {
+  using T = typename M::T;
+  constexpr unsigned kFull = 0xffffffffu;
+  const int n0 = L.n[0], n1 = L.n[1], n2 = L.n[2];
+  const int lane = threadIdx.x;
+  const int x0 = (blockIdx.x * 32 + lane) * 4;
+  const bool active = x0 < n2;
+  const int y0 = (blockIdx.y * BW + threadIdx.y) * RY;   // first source row (warp-uniform)
+  const int p0 = blockIdx.z;                             // source plane
+  const int xl2 = x0 >= 2 ? x0 - 2 : x0 - 2 + n2;        // lane 0's left neighbours
+  const int xl1 = x0 >= 1 ? x0 - 1 : x0 - 1 + n2;
+  auto row_at = [&](int p, int y) -> uint32_t { return ((uint32_t)p * (uint32_t)n1 + (uint32_t)y) * (uint32_t)n2; };
+  // window x0-2 .. x0+3 of one row (all lanes take part in the shuffles)
+  auto window = [&](const S* a, float scale, uint32_t row, T w[6], bool left) {
+    T v[4] = {T(0), T(0), T(0), T(0)};
+    if (active) Quad<S>::get(a + row + x0, scale, v);
+    T l2 = T(0), l3 = T(0);
+    if (left) {
+      l2 = __shfl_up_sync(kFull, v[2], 1);
+      l3 = __shfl_up_sync(kFull, v[3], 1);
+      if (lane == 0 && active) {
+        l2 = Storage<S, T>::load(ro_load(a + row + xl2), scale);
+        l3 = Storage<S, T>::load(ro_load(a + row + xl1), scale);
+      }
+    }
+    w[0] = l2;
+    w[1] = l3;
+#pragma unroll
+    for (int i = 0; i < 4; ++i) w[2 + i] = v[i];
+  };
+  const int pm = p0 > 0 ? p0 - 1 : n0 - 1, pp = p0 + 1 < n0 ? p0 + 1 : 0;
+  T c[NF][RY + 2][6];
+  T z[NF][2][RY][4];
+#pragma unroll
+  for (int f = 0; f < NF; ++f) {
+    const S* a = static_cast<const S*>(L.in[f]);
+    const float sc = L.scale[f];
+#pragma unroll
+    for (int r = -1; r <= RY; ++r) window(a, sc, row_at(p0, pmod(y0 + r, n1)), c[f][r + 1], true);
+#pragma unroll
+    for (int r = 0; r < RY; ++r) {
+      const int y = pmod(y0 + r, n1);
+#pragma unroll
+      for (int d = 0; d < 2; ++d) {
+        T w[6];
+        window(a, sc, row_at(d ? pp : pm, y), w, true);   // x0-2 .. x0+3; the sources are x0-1 .. x0+2
+#pragma unroll
+        for (int i = 0; i < 4; ++i) z[f][d][r][i] = w[1 + i];
+      }
+    }
+  }
+  T out[NF][RY][4];
+  const typename M::U* U = static_cast<const typename M::U*>(L.uniforms);
+  static_for(std::make_integer_sequence<int, RY>{}, [&](auto rc) {
+    constexpr int R = decltype(rc)::value;
+    static_for(std::make_integer_sequence<int, 4>{}, [&](auto ec) {
+      constexpr int E = decltype(ec)::value;
+      QuadAccess<T, NF, RY, R, E> acc{c, z, out};
+      eval<M, Stage>(acc, U);
+    });
+  });
+  if (!active) return;
+#pragma unroll
+  for (int r = 0; r < RY; ++r) {
+    if (y0 + r >= n1) break;
+    const int yd = y0 + r + 1 < n1 ? y0 + r + 1 : 0;    // rolled by one point (y0 + r < n1)
+#pragma unroll
+    for (int f = 0; f < NF; ++f)
+      Quad<S>::put(static_cast<S*>(L.out[f]) + row_at(pp, yd) + x0, out[f][r], L.inv_scale[f]);
+  }
+}
+
+template <class Prog, int P, class Stage, int RY, int BW>
+struct Quad3dVariant {
+  using M = typename Precision<P>::M;
+  using S = typename Precision<P>::S;
+  static cudaError_t launch(const FgbLaunch* L, cudaStream_t stream) {
+    const dim3 grid((L->n[2] + 127) / 128, (L->n[1] + BW * RY - 1) / (BW * RY), L->n[0]);
+    quad3d_kernel<M, S, Stage, Prog::kFields, RY, BW><<<grid, dim3(32, BW), 0, stream>>>(*L);
+    return cudaGetLastError();
+  }
+  static FgbFusedVariant describe() {
+    FgbFusedVariant v;
+    v.x_multiple = 4;
+    v.launch = &launch;
+    v.tile_x = 128;
+    v.tile_y = BW * RY;
+    v.steps = 1;
+    v.smem_bytes = 0;
     return v;
   }
 };

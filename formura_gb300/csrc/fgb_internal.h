@@ -44,6 +44,7 @@ struct FgbFusedVariant {
   FgbStageLaunch launch;
   int tile_x, tile_y, steps;
   size_t smem_bytes;
+  int x_multiple;          // the contiguous axis must be a multiple of this
 };
 
 // Batched ensembles: many independent 2D grids of one single-stage program,

@@ -476,14 +476,16 @@ static bool variant_fits(const fgb_grid* g, int index) {
   int dev = 0, optin = 0;
   cudaGetDevice(&dev);
   cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-  return g->prog->fused[g->precision][index].smem_bytes <= (size_t)optin;
+  const FgbFusedVariant& v = g->prog->fused[g->precision][index];
+  return v.smem_bytes <= (size_t)optin && (v.x_multiple <= 1 || g->n[2] % v.x_multiple == 0);
 }
 
 int fgb_set_variant(fgb_grid* g, int index) {
   if (!g || index < -1 || index >= g->prog->nfused[g->precision]) return fail(FGB_E_ARG, "no such variant");
   if (index >= 0 && !variant_fits(g, index))
-    return fail(FGB_E_ARG, "variant %d needs %zu bytes of shared memory", index,
-                g->prog->fused[g->precision][index].smem_bytes);
+    return fail(FGB_E_ARG, "variant %d does not fit this grid (it needs %zu bytes of shared memory and "
+                "a contiguous axis that is a multiple of %d)", index,
+                g->prog->fused[g->precision][index].smem_bytes, g->prog->fused[g->precision][index].x_multiple);
   if (index != g->variant && g->graph) {
     cudaGraphExecDestroy(g->graph);
     g->graph = nullptr;

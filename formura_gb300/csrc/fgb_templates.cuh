@@ -563,8 +563,15 @@ struct FusedFill {
           Tb3dVariant<Prog, P, Stage0, 64 - 4 * R, 24, 2>::describe(),
           Tb3dVariant<Prog, P, Stage0, 64 - 16 * R, 16, 8>::describe(),
       };
-      d.nfused[P] = (int)(sizeof v / sizeof v[0]);
-      for (int i = 0; i < d.nfused[P]; ++i) d.fused[P][i] = v[i];
+      int count = (int)(sizeof v / sizeof v[0]);
+      for (int i = 0; i < count; ++i) d.fused[P][i] = v[i];
+      // one step per launch on four-point row vectors (FP32 and FP16 storage,
+      // star stencils of reach 1 rolled by one point)
+      if constexpr ((P == 2 || P == 3) && Prog::kStar && Prog::kReach == 1 && Prog::kShift == 1) {
+        d.fused[P][count++] = Quad3dVariant<Prog, P, Stage0, 2, 4>::describe();
+        d.fused[P][count++] = Quad3dVariant<Prog, P, Stage0, 4, 2>::describe();
+      }
+      d.nfused[P] = count;
       d.nbatch[P] = 0;
     } else {
       d.nfused[P] = 0;

@@ -551,11 +551,15 @@ class _ProgramEmitter:
                 "reference's loop nest would write outside the grid")
         self.shift = 2 * s - offs.pop()
         reach = 0
+        star = True
         for n in self.mmg:
             for mn in n.micro:
                 if mn.inst[0] in ("loadstatic", "loadcursor"):
                     reach = max(reach, max(abs(x) for x in mn.inst[1]))
+                    star = star and sum(1 for x in mn.inst[1] if x != 0) <= 1
         self.reach = reach
+        # every load moves along at most one axis
+        self.star = star
 
     def cursor3(self, c) -> List[int]:
         c = list(c)
@@ -619,6 +623,7 @@ class _ProgramEmitter:
                    f"  static constexpr int kSleeve = {self.sleeve};\n"
                    f"  static constexpr int kShift = {self.shift};\n"
                    f"  static constexpr int kReach = {self.reach};\n"
+                   f"  static constexpr bool kStar = {'true' if self.star else 'false'};\n"
                    f"  static constexpr int kUniforms = {len(self.table)};\n"
                    f"  // uniform-table slots of the divisors (-1: a literal divisor)\n"
                    f"  static constexpr int kNumDivisors = {div_count};\n"

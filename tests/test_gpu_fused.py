@@ -107,3 +107,30 @@ def test_3d_streaming_variants_match_single_steps(shape, prec):
         assert bits_equal(got, ref), v
     assert tried >= 3
     g.close()
+
+
+@pytest.mark.parametrize("shape", [(48, 48, 48), (8, 40, 36), (40, 72, 128), (3, 5, 4), (20, 9, 260)])
+def test_3d_one_step_variants_match_in_f16(shape):
+    """With FP16 storage every step stores half values, so the one-step
+    variants (four-point row vectors) equal the generic stage kernel bit for
+    bit as well; the multi-step tiles keep FP32 values between their steps
+    and are left out here."""
+    src, _ = builtin_program("heat3d")
+    _, U = program_uniforms(src, W.heat_config(shape[2]), "heat3d")
+    x = np.random.default_rng(6).random((1,) + shape)
+    steps = 13
+    g = Grid("heat3d", shape, "f16", U, scales=[1.0])
+    g.upload(x)
+    g.forward(steps)
+    ref = g.download()
+    tried = 0
+    for v in g.variants():
+        if v["steps"] != 1:
+            continue
+        g.upload(x)
+        g.set_variant(v["index"])
+        tried += 1
+        g.forward(steps)
+        assert bits_equal(g.download(), ref), v
+    assert tried >= 2
+    g.close()
