@@ -519,10 +519,12 @@ def run_ours(args, spec):
     e2e_sampler.start()
     e2e_calls = max(1, min(args.steps, args.e2e_steps))
     e2e_s = 0.0
+    call_ms = []
     for c in range(e2e_calls):
         t0 = time.perf_counter()
         dp.forward(1)
-        e2e_s += time.perf_counter() - t0
+        call_ms.append((time.perf_counter() - t0) * 1e3)
+        e2e_s += call_ms[-1] / 1e3
         if vgrids:
             ref = [dp.get(f) for f in dp.fields]
             for p, gv in vgrids.items():
@@ -533,6 +535,7 @@ def run_ours(args, spec):
            "h2d_bytes_per_step": nf * cells * 8, "d2h_bytes_per_step": nf * cells * 8,
            "steps": e2e_calls, "time_steps": e2e_calls * spf,
            "api": "Formura_Forward (drop-in C API, formura_data on the host)",
+           "call_ms": [round(x, 2) for x in call_ms],
            "clocks": e2e_sampler.stop()}
     for p, gv in vgrids.items():
         above = [s for s, e in track[p] if e > BOUNDS[p]]

@@ -138,7 +138,7 @@ RUNTIME_UNITS = ("fgb_runtime", "fgb_noalloc", "fgb_batch", "fgb_lazy")
 
 
 def _deps() -> List[str]:
-    return [os.path.join(CSRC, f) for f in ("fgb_internal.h", "fgb_templates.cuh", "fgb_fused.cuh", "fgb_wait.cuh")
+    return [os.path.join(CSRC, f) for f in ("fgb_internal.h", "fgb_templates.cuh", "fgb_fused.cuh", "fgb_fused_ms.cuh", "fgb_wait.cuh")
             if os.path.exists(os.path.join(CSRC, f))] + [os.path.join(ROOT, "include", "formura_gb300.h")]
 
 

@@ -786,3 +786,5 @@ struct Quad3dVariant {
 };
 
 }  // namespace fgb
+
+#include "fgb_fused_ms.cuh"

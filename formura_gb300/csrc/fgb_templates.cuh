@@ -573,6 +573,17 @@ struct FusedFill {
       }
       d.nfused[P] = count;
       d.nbatch[P] = 0;
+    } else if constexpr (Prog::kDim == 3 && Prog::kStages > 1 && (P == 2 || P == 3)) {
+      // multi-stage steps in one launch, the stages' arrays in shared memory
+      const FgbFusedVariant v[] = {
+          Ms3dVariant<Prog, P, 16, 16, Stage0, Rest...>::describe(),
+          Ms3dVariant<Prog, P, 12, 12, Stage0, Rest...>::describe(),
+          Ms3dVariant<Prog, P, 8, 16, Stage0, Rest...>::describe(),
+          Ms3dVariant<Prog, P, 8, 8, Stage0, Rest...>::describe(),
+      };
+      d.nfused[P] = (int)(sizeof v / sizeof v[0]);
+      for (int i = 0; i < d.nfused[P]; ++i) d.fused[P][i] = v[i];
+      d.nbatch[P] = 0;
     } else {
       d.nfused[P] = 0;
       d.nbatch[P] = 0;

@@ -561,6 +561,46 @@ class _ProgramEmitter:
         # every load moves along at most one axis
         self.star = star
 
+    def stage_reads(self) -> str:
+        """Where each stage reads: the lowest and highest offset per axis of
+        its state loads, and of its loads of the arrays of every earlier
+        stage (lo > hi: no such load).  The fused multi-stage kernels size
+        their shared-memory windows from these."""
+        ns = len(self.stages)
+        stage_of = {n.omid: st.index for st in self.stages for n in st.nodes}
+        big = 1 << 20
+        slo = [[big] * 3 for _ in range(ns)]
+        shi = [[-big] * 3 for _ in range(ns)]
+        rlo = [[[big] * 3 for _ in range(ns)] for _ in range(ns)]
+        rhi = [[[-big] * 3 for _ in range(ns)] for _ in range(ns)]
+        for st in self.stages:
+            c = st.index
+            for node in st.nodes:
+                for mn in node.micro:
+                    k = mn.inst[0]
+                    if k == "loadstatic":
+                        lo, hi = slo[c], shi[c]
+                    elif k == "loadcursor" and stage_of[mn.inst[2]] != c:
+                        lo, hi = rlo[c][stage_of[mn.inst[2]]], rhi[c][stage_of[mn.inst[2]]]
+                    else:
+                        continue
+                    for a, x in enumerate(self.cursor3(mn.inst[1])):
+                        lo[a] = min(lo[a], x)
+                        hi[a] = max(hi[a], x)
+        mid_stage = [stage_of[m] for m in self.mids] or [0]
+
+        def arr(v):
+            if isinstance(v, list):
+                return "{" + ", ".join(arr(x) for x in v) + "}"
+            return str(v)
+        return (f"struct StageReads {{\n"
+                f"  static constexpr int kMidStage[{len(mid_stage)}] = {arr(mid_stage)};\n"
+                f"  static constexpr int kStateLo[{ns}][3] = {arr(slo)};\n"
+                f"  static constexpr int kStateHi[{ns}][3] = {arr(shi)};\n"
+                f"  static constexpr int kReadLo[{ns}][{ns}][3] = {arr(rlo)};\n"
+                f"  static constexpr int kReadHi[{ns}][{ns}][3] = {arr(rhi)};\n"
+                f"}};\n")
+
     def cursor3(self, c) -> List[int]:
         c = list(c)
         return [0] * (3 - len(c)) + c
@@ -587,6 +627,7 @@ class _ProgramEmitter:
             body = "\n".join(se.lines)
             stage_texts.append(
                 f"struct Stage{st.index} {{\n"
+                f"  static constexpr int kIndex = {st.index};\n"
                 f"  static constexpr bool kWritesState = {'true' if st.writes_state else 'false'};\n"
 
                 f"  static constexpr int kMidOut = {len(st.mid_out)};\n"
@@ -613,6 +654,7 @@ class _ProgramEmitter:
         div_slots = sorted(self.divisor_slots) if self.divisor_slots is not None else []
         div_count = len(div_slots) if self.divisor_slots is not None else -1
         div_list = ", ".join(str(i) for i in div_slots) if div_slots else "0"
+        out.append(self.stage_reads())
         out.append(f"struct Prog {{\n"
                    f"  using Adjoint = {'AdjointStep' if adj_src else 'void'};\n"
                    f"  using StageAdjoint = {'StageAdjointList' if stage_adj else 'void'};\n"
@@ -624,6 +666,7 @@ class _ProgramEmitter:
                    f"  static constexpr int kShift = {self.shift};\n"
                    f"  static constexpr int kReach = {self.reach};\n"
                    f"  static constexpr bool kStar = {'true' if self.star else 'false'};\n"
+                   f"  using Reads = StageReads;\n"
                    f"  static constexpr int kUniforms = {len(self.table)};\n"
                    f"  // uniform-table slots of the divisors (-1: a literal divisor)\n"
                    f"  static constexpr int kNumDivisors = {div_count};\n"

@@ -96,6 +96,11 @@ class Library:
         self.check(self.lib.fgb_program_query(program.encode(), *[ctypes.byref(v) for v in vals]), "query")
         return dict(zip(["dim", "nfields", "nuniforms", "sleeve", "shift"], [v.value for v in vals]))
 
+    def fields(self, program: str) -> List[str]:
+        """The program's state fields in formura_data order."""
+        n = self.query(program)["nfields"]
+        return [self.lib.fgb_program_field(program.encode(), i).decode() for i in range(n)]
+
 
 class Grid:
     """One device-resident grid of a program compiled into the library."""

@@ -7,7 +7,7 @@ import numpy as np
 import pytest
 
 from formura_gb300 import workloads as W
-from formura_gb300.host import Grid, builtin_program, program_uniforms
+from formura_gb300.host import Grid, Library, builtin_program, program_uniforms
 from conftest import bits_equal
 
 pytestmark = pytest.mark.gpu
@@ -129,6 +129,40 @@ def test_3d_one_step_variants_match_in_f16(shape):
             continue
         g.upload(x)
         g.set_variant(v["index"])
+        tried += 1
+        g.forward(steps)
+        assert bits_equal(g.download(), ref), v
+    assert tried >= 2
+    g.close()
+
+
+@pytest.mark.parametrize("program,shape", [("hllc3d", (24, 24, 24)), ("hllc3d", (20, 30, 18)),
+                                           ("hllc3d", (7, 9, 13)), ("hllc3d", (40, 16, 33)),
+                                           ("hlld3d", (12, 14, 10))])
+@pytest.mark.parametrize("prec", ["f32", "f16"])
+def test_multistage_fused_variants_match_stage_kernels(program, shape, prec):
+    """The one-launch multi-stage kernels (every stage's arrays in
+    shared-memory plane rings, 2.5D streaming) equal the stage-per-kernel
+    path bit for bit, for every tile shape that fits."""
+    src, _ = builtin_program(program)
+    cfg = {"hllc3d": W.hllc_config, "hlld3d": W.mhd_config}[program](shape[2])
+    _, U = program_uniforms(src, cfg, program)
+    st = (W.hllc_state if program == "hllc3d" else W.mhd_state)(shape, seed=4)
+    fields = Library.get().fields(program)
+    x = np.stack([st[f] for f in fields])
+    sc = [float(max(1e-3, np.abs(x[i]).max())) for i in range(len(fields))] if prec == "f16" else None
+    steps = 9
+    g = Grid(program, shape, prec, U, scales=sc)
+    g.upload(x)
+    g.forward(steps)
+    ref = g.download()
+    tried = 0
+    for v in g.variants():
+        g.upload(x)
+        try:
+            g.set_variant(v["index"])
+        except Exception:
+            continue            # needs more shared memory than this device has
         tried += 1
         g.forward(steps)
         assert bits_equal(g.download(), ref), v
