@@ -15,8 +15,10 @@
 // The halo and ring depths follow from where each stage reads the arrays of
 // the earlier stages and the state (the generator's StageReads table).  The
 // stage functors are the generated ones, unchanged: they see an accessor
-// that maps array and state loads to the shared-memory rings.  Results are
-// those of the stage-per-kernel path, bit for bit.
+// that maps array and state loads to the shared-memory rings.  Every tile
+// shape gives the same bits; against the stage-per-kernel path the FP32
+// results agree to rounding, since nvcc contracts products and sums into
+// FMAs differently in the two kernels.
 #pragma once
 
 namespace fgb {
