@@ -123,6 +123,52 @@ struct F64Exact {
     const T e = __fma_rn(-q, c, x);
     return is_zero(x) ? q : __fma_rn(e, y, q);
   }
+  // The last rounding step of that quotient on the integer pipe, in place of
+  // Markstein's second FMA.  With q0 = RN(x * y) and the exact remainder
+  // r = x - q0*c: x*y is within |x/c| * 2^-53 of x/c, so where q0 lies at
+  // least two ulps inside its binade, x/c lies in the same binade within
+  // 1.5 ulp of q0, and RN(x/c) is q0 or the neighbour towards x/c (the sign
+  // of r/c).  It is the neighbour when |r| > |c| * ulp(q0) / 2 (a quotient of
+  // two doubles is never exactly a midpoint; the even one is taken if it
+  // were).  |c| * ulp(q0) / 2 is |c| with its exponent field moved, and two
+  // non-negative doubles compare like their bit patterns.  A neighbour is
+  // the bit pattern plus or minus one inside the binade.  Where |r| is below
+  // the threshold it is exact or, under 2^-1022, smaller than the threshold
+  // whatever its rounding (the threshold is kept at least 2^-1021).
+  // `fits` reports whether the step applies; zero numerators keep RN(x*y).
+  static __device__ __forceinline__ T round_quotient(T x, T c, T q0, T r, bool& fits) {
+    unsigned qlo, qhi, rlo, rhi, clo, chi;
+    halves(q0, qlo, qhi);
+    halves(r, rlo, rhi);
+    halves(c, clo, chi);
+    const unsigned eq = (qhi >> 20) & 0x7ffu, ec = (chi >> 20) & 0x7ffu;
+    const unsigned long long m = ((unsigned long long)(qhi & 0xfffffu) << 32) | qlo;
+    const int et = (int)ec + (int)eq - 1076;   // exponent field of |c| * ulp(q0) / 2
+    const bool zero = is_zero(x);
+    fits = zero || (m - 2ull <= (1ull << 52) - 5ull && (unsigned)(et - 2) <= 2044u);
+    const unsigned long long t = ((unsigned long long)((chi & 0xfffffu) | ((unsigned)et << 20)) << 32) | clo;
+    const unsigned long long a = ((unsigned long long)(rhi & 0x7fffffffu) << 32) | rlo;
+    const bool step = a > t || (a == t && (qlo & 1u));
+    const bool up = ((rhi ^ chi ^ qhi) >> 31) == 0;   // towards x/c the magnitude grows
+    const unsigned long long qb = ((unsigned long long)qhi << 32) | qlo;
+    const unsigned long long res = qb + (step ? (up ? 1ull : ~0ull) : 0ull);
+    return zero ? q0 : join((unsigned)res, (unsigned)(res >> 32));
+  }
+  // RN(x / c) inside Markstein's window: two FP64 instructions and the
+  // integer step where it applies to every lane of the warp, else
+  // Markstein's second FMA (the same bits).
+  static __device__ __forceinline__ T quotient(T x, T c, T y) {
+    const T q0 = __dmul_rn(x, y);
+    const T r = __fma_rn(-q0, c, x);
+    bool fits;
+    const T q = round_quotient(x, c, q0, r, fits);
+    if (warp_all(fits)) return q;
+    return markstein_last(x, q0, r, y);
+  }
+  // out of line, so that the compiler does not compute it ahead of the test
+  static __device__ __noinline__ T markstein_last(T x, T q0, T r, T y) {
+    return is_zero(x) ? q0 : __fma_rn(r, y, q0);
+  }
   // The divisions decide per operation instead of raising the flag: a field
   // that decays through the subnormal range (Gray-Scott's v far from the
   // pattern) keeps whole warps out of the window for many steps, and there
@@ -141,7 +187,7 @@ struct F64Exact {
     (void)rc;
     return __ddiv_rn(x, c);
 #else
-    if (warp_all(divu_window(x, c))) return markstein(x, c, rc);
+    if (warp_all(divu_window(x, c))) return quotient(x, c, rc);
     return divu_outside(x, c, rc);
 #endif
   }
@@ -172,7 +218,7 @@ struct F64Exact {
     return within(b, 400) && (is_zero(a) || within(a, 400));
   }
   static __device__ __forceinline__ T divr(T a, T b, T y, bool&) {
-    if (warp_all(divr_window(a, b))) return markstein(a, b, y);
+    if (warp_all(divr_window(a, b))) return quotient(a, b, y);
     return __ddiv_rn(a, b);
   }
   static __device__ __forceinline__ T neg(T a) { return -a; }

@@ -46,9 +46,10 @@ __device__ __forceinline__ bool same(double a, double b) {
 // to the IEEE division by itself); the multiply-add wherever its range flag
 // stays set (where it drops, the kernels evaluate with F64Ieee instead).
 // Counts per operation: mismatches, and lanes inside the shortened window;
-// then the mismatches of the integer-pipe comparisons.
+// then the mismatches of the integer-pipe comparisons, and of the divisions'
+// integer rounding step taken lane by lane, with the lanes it applied to.
 __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
-  unsigned long long bad[4] = {0, 0, 0, 0}, fast[3] = {0, 0, 0};
+  unsigned long long bad[4] = {0, 0, 0, 0}, fast[3] = {0, 0, 0}, step_used = 0, step_bad = 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
     const uint64_t key = seed * 0x100000000ull + i;
@@ -67,6 +68,15 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
     double r = F64Exact::divu(x, c, rc, ok);
     fast[0] += F64Exact::divu_window(x, c);
     bad[0] += ok && !same(r, __ddiv_rn(x, c));
+    // the integer rounding step on its own, lane by lane (the kernels take it
+    // only where every lane of a warp fits)
+    if (F64Exact::divu_window(x, c)) {
+      const double q0 = __dmul_rn(x, rc), rem = __fma_rn(-q0, c, x);
+      bool fits;
+      const double q = F64Exact::round_quotient(x, c, q0, rem, fits);
+      step_used += fits;
+      step_bad += fits && !same(q, __ddiv_rn(x, c));
+    }
     // divr: grid numerator and denominator
     const double a = operand(key * 7 + 2, ca == 5 ? (int)(mix(key ^ 1) % 6) : ca);
     const double b = operand(key * 7 + 3, cb);
@@ -74,6 +84,13 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
     r = F64Exact::divr(a, b, F64Exact::rcp(b), ok);
     fast[1] += F64Exact::divr_window(a, b);
     bad[1] += ok && !same(r, __ddiv_rn(a, b));
+    if (F64Exact::divr_window(a, b)) {
+      const double y = F64Exact::rcp(b), q0 = __dmul_rn(a, y), rem = __fma_rn(-q0, b, a);
+      bool fits;
+      const double q = F64Exact::round_quotient(a, b, q0, rem, fits);
+      step_used += fits;
+      step_bad += fits && !same(q, __ddiv_rn(a, b));
+    }
     // fma with a = +-2^k, k in [-3, 3]: RN(RN(a*h) + t)
     const int k = (int)(mix(warp * 7 + seed) % 7) - 3;
     const double f = ((warp & 1) ? -1.0 : 1.0) * ldexp(1.0, k);
@@ -97,15 +114,17 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
     atomicAdd(&out[3 + j], fast[j]);
   }
   atomicAdd(&out[6], bad[3]);
+  atomicAdd(&out[7], step_bad);
+  atomicAdd(&out[8], step_used);
 }
 
 extern "C" int exact_forms_gpu_check(unsigned long long seed, unsigned long long n, unsigned long long* host_out) {
   unsigned long long* d = nullptr;
-  if (cudaMalloc(&d, 7 * sizeof(unsigned long long)) != cudaSuccess) return 1;
-  cudaMemset(d, 0, 7 * sizeof(unsigned long long));
+  if (cudaMalloc(&d, 9 * sizeof(unsigned long long)) != cudaSuccess) return 1;
+  cudaMemset(d, 0, 9 * sizeof(unsigned long long));
   check<<<152 * 8, 256>>>(seed, n, d);
   cudaError_t e = cudaDeviceSynchronize();
-  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 7 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 9 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
   cudaFree(d);
   return e == cudaSuccess ? 0 : 2;
 }

