@@ -701,21 +701,20 @@ __global__ void __launch_bounds__(32 * BW) quad3d_kernel(const __grid_constant__
   const bool active = x0 < n2;
   const int y0 = (blockIdx.y * BW + threadIdx.y) * RY;   // first source row (warp-uniform)
   const int p0 = blockIdx.z;                             // source plane
-  const int xl2 = x0 >= 2 ? x0 - 2 : x0 - 2 + n2;        // lane 0's left neighbours
-  const int xl1 = x0 >= 1 ? x0 - 1 : x0 - 1 + n2;
+  const int xl4 = x0 >= 4 ? x0 - 4 : x0 - 4 + n2;        // lane 0's left vector x0-4 .. x0-1
   auto row_at = [&](int p, int y) -> uint32_t { return ((uint32_t)p * (uint32_t)n1 + (uint32_t)y) * (uint32_t)n2; };
-  // window x0-2 .. x0+3 of one row (all lanes take part in the shuffles)
-  auto window = [&](const S* a, float scale, uint32_t row, T w[6], bool left) {
+  // window x0-2 .. x0+3 of one row (all lanes take part in the shuffles;
+  // lane 0 loads the vector to its left)
+  auto window = [&](const S* a, float scale, uint32_t row, T w[6]) {
     T v[4] = {T(0), T(0), T(0), T(0)};
     if (active) Quad<S>::get(a + row + x0, scale, v);
-    T l2 = T(0), l3 = T(0);
-    if (left) {
-      l2 = __shfl_up_sync(kFull, v[2], 1);
-      l3 = __shfl_up_sync(kFull, v[3], 1);
-      if (lane == 0 && active) {
-        l2 = Storage<S, T>::load(ro_load(a + row + xl2), scale);
-        l3 = Storage<S, T>::load(ro_load(a + row + xl1), scale);
-      }
+    T l2 = __shfl_up_sync(kFull, v[2], 1);
+    T l3 = __shfl_up_sync(kFull, v[3], 1);
+    if (lane == 0 && active) {
+      T u[4];
+      Quad<S>::get(a + row + xl4, scale, u);
+      l2 = u[2];
+      l3 = u[3];
     }
     w[0] = l2;
     w[1] = l3;
@@ -723,6 +722,11 @@ __global__ void __launch_bounds__(32 * BW) quad3d_kernel(const __grid_constant__
     for (int i = 0; i < 4; ++i) w[2 + i] = v[i];
   };
   const int pm = p0 > 0 ? p0 - 1 : n0 - 1, pp = p0 + 1 < n0 ? p0 + 1 : 0;
+  // rows y0-1 .. y0+RY, wrapped: one division, then steps
+  int yr[RY + 2];
+  yr[0] = pmod(y0 - 1, n1);
+#pragma unroll
+  for (int r = 1; r < RY + 2; ++r) yr[r] = yr[r - 1] + 1 == n1 ? 0 : yr[r - 1] + 1;
   T c[NF][RY + 2][6];
   T z[NF][2][RY][4];
 #pragma unroll
@@ -730,14 +734,13 @@ __global__ void __launch_bounds__(32 * BW) quad3d_kernel(const __grid_constant__
     const S* a = static_cast<const S*>(L.in[f]);
     const float sc = L.scale[f];
 #pragma unroll
-    for (int r = -1; r <= RY; ++r) window(a, sc, row_at(p0, pmod(y0 + r, n1)), c[f][r + 1], true);
+    for (int r = 0; r < RY + 2; ++r) window(a, sc, row_at(p0, yr[r]), c[f][r]);
 #pragma unroll
     for (int r = 0; r < RY; ++r) {
-      const int y = pmod(y0 + r, n1);
 #pragma unroll
       for (int d = 0; d < 2; ++d) {
         T w[6];
-        window(a, sc, row_at(d ? pp : pm, y), w, true);   // x0-2 .. x0+3; the sources are x0-1 .. x0+2
+        window(a, sc, row_at(d ? pp : pm, yr[r + 1]), w);   // x0-2 .. x0+3; the sources are x0-1 .. x0+2
 #pragma unroll
         for (int i = 0; i < 4; ++i) z[f][d][r][i] = w[1 + i];
       }
@@ -781,6 +784,221 @@ struct Quad3dVariant {
     v.tile_y = BW * RY;
     v.steps = 1;
     v.smem_bytes = 0;
+    return v;
+  }
+};
+
+
+// ---------------------------------------------------------------------------
+// One step of a 3D single-stage program, marching along z through shared memory
+// ---------------------------------------------------------------------------
+// The same programs and the same four-point row vectors as quad3d_kernel,
+// but a CTA walks a chunk of planes and every plane of its tile (with one
+// row above and below and four points to the left) arrives once, by
+// cp.async into a ring of shared-memory slots, P planes ahead of the plane
+// being updated.  A thread then reads its centre window (x0-2 .. x0+3 of
+// rows y-1 .. y+RY) and its rows of the planes z-1 and z+1 from shared
+// memory.  L2 serves each value about (rows + 2) / rows times instead of
+// the one-plane kernel's three and a quarter, and the copies in flight do
+// not hold registers.  Results are the generic stage kernel's.
+template <class S>
+__device__ __forceinline__ void cp_async4(S* dst, const S* src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  if constexpr (sizeof(S) == 4)
+    asm volatile("cp.async.cg.shared.global [%0], [%1], 16;\n" ::"r"(d), "l"(src) : "memory");
+  else
+    asm volatile("cp.async.ca.shared.global [%0], [%1], 8;\n" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;\n" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() { asm volatile("cp.async.wait_group %0;\n" ::"n"(N) : "memory"); }
+
+// four consecutive storage elements from shared memory (aligned)
+template <class S> struct QuadSm;
+template <> struct QuadSm<float> {
+  static __device__ __forceinline__ void get(const float* p, float, float v[4]) {
+    const float4 q = *reinterpret_cast<const float4*>(p);
+    v[0] = q.x;
+    v[1] = q.y;
+    v[2] = q.z;
+    v[3] = q.w;
+  }
+};
+template <> struct QuadSm<__half> {
+  static __device__ __forceinline__ void get(const __half* p, float scale, float v[4]) {
+    const uint2 q = *reinterpret_cast<const uint2*>(p);
+    __half h[4];
+    memcpy(h, &q, sizeof q);
+#pragma unroll
+    for (int i = 0; i < 4; ++i) v[i] = Storage<__half, float>::load(h[i], scale);
+  }
+};
+
+template <class S, int NF, int RY, int BW, int P>
+struct ZringLayout {
+  static constexpr int kRows = BW * RY + 2;        // the tile's rows and one row either side
+  static constexpr int kRow = 132;                 // x_lo-4 .. x_lo+127
+  static constexpr int kSlots = P + 3;             // planes z-1, z, z+1 and P ahead
+  static constexpr int kPlane = NF * kRows * kRow; // elements of one slot
+  static constexpr size_t kBytes = (size_t)kSlots * kPlane * sizeof(S);
+};
+
+template <class M, class S, class Stage, int NF, int RY, int BW, int P>
+__global__ void __launch_bounds__(32 * BW) zring3d_kernel(const __grid_constant__ FgbLaunch L) {
+  using T = typename M::T;
+  using Lay = ZringLayout<S, NF, RY, BW, P>;
+  constexpr int NS = Lay::kSlots, ROWS = Lay::kRows, RW = Lay::kRow;
+  extern __shared__ __align__(16) unsigned char zr_smem[];
+  S* sm = reinterpret_cast<S*>(zr_smem);
+  const int n0 = L.n[0], n1 = L.n[1], n2 = L.n[2];
+  const int lane = threadIdx.x, w = threadIdx.y, tid = w * 32 + lane;
+  const int xlo = blockIdx.x * 128, ylo = blockIdx.y * (BW * RY);
+  const int chunk = (n0 + gridDim.z - 1) / gridDim.z;
+  const int za = blockIdx.z * chunk, zb = za + chunk < n0 ? za + chunk : n0;
+  if (za >= zb) return;
+  // four-point pieces of one plane: per row, the left halo piece
+  // (x_lo-4 .. x_lo-1, wrapped) and the 32 pieces of x_lo .. x_lo+127.  A
+  // thread copies the same pieces of every plane and field: their offsets
+  // within a plane (global and in its slot) are formed once.
+  constexpr int kPieces = ROWS * 33, kMine = (kPieces + 32 * BW - 1) / (32 * BW);
+  uint32_t src_off[kMine];
+  int dst_off[kMine];
+#pragma unroll
+  for (int j = 0; j < kMine; ++j) {
+    const int i = tid + j * 32 * BW;
+    const int r = i / 33, k = i - r * 33;
+    const int x = k == 0 ? (xlo == 0 ? n2 - 4 : xlo - 4) : xlo + 4 * (k - 1);
+    // pieces past the rows or right of the grid are not copied (the
+    // columns right of the grid are read by idle lanes only)
+    dst_off[j] = i < kPieces && x < n2 ? r * RW + 4 * k : -1;
+    src_off[j] = (uint32_t)pmod(ylo - 1 + r, n1) * (uint32_t)n2 + (uint32_t)x;
+  }
+  const uint32_t plane_elems = (uint32_t)n1 * (uint32_t)n2;
+  auto issue = [&](int q) {   // plane q (unwrapped, za-1 <= q) into its slot
+    const int slot = (q - za + 1) % NS;
+    const uint32_t base = (uint32_t)pmod(q, n0) * plane_elems;   // P may exceed the grid's depth
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      const S* a = static_cast<const S*>(L.in[f]) + base;
+      S* d = sm + (size_t)slot * Lay::kPlane + f * ROWS * RW;
+#pragma unroll
+      for (int j = 0; j < kMine; ++j)
+        if (dst_off[j] >= 0) cp_async4(d + dst_off[j], a + src_off[j]);
+    }
+    cp_async_commit();
+  };
+  // prologue: planes za-1, za, then za+1 .. za+P, one group each
+  issue(za - 1);
+  issue(za);
+#pragma unroll 1
+  for (int q = za + 1; q <= za + P; ++q) issue(q);
+  const int x0 = xlo + 4 * lane;
+  const bool active = x0 < n2;
+  const int yt = ylo + w * RY;   // the thread's first row (source)
+  const typename M::U* U = static_cast<const typename M::U*>(L.uniforms);
+#pragma unroll 1
+  for (int p = za; p < zb; ++p) {
+    cp_async_wait<P - 1>();   // planes up to p+1 have landed (this thread's pieces)
+    __syncthreads();          // ... everyone's, and plane p-2's slot is free
+    issue(p + 1 + P);         // (beyond the chunk the copies are unused but harmless)
+    const S* cz = sm + (size_t)((p - za + 1) % NS) * Lay::kPlane;
+    const S* zm = sm + (size_t)((p - za) % NS) * Lay::kPlane;
+    const S* zp = sm + (size_t)((p - za + 2) % NS) * Lay::kPlane;
+    // each row: the thread's vector x0 .. x0+3, and the values to its left
+    // from the lane on the left (lane 0: from the row's halo)
+    T c[NF][RY + 2][6];
+    T z[NF][2][RY][4];
+#pragma unroll
+    for (int f = 0; f < NF; ++f) {
+      const float sc = L.scale[f];
+#pragma unroll
+      for (int r = 0; r < RY + 2; ++r) {
+        const S* row = cz + (f * ROWS + w * RY + r) * RW;
+        T v[4];
+        QuadSm<S>::get(row + 4 + 4 * lane, sc, v);
+        T l2 = __shfl_up_sync(0xffffffffu, v[2], 1), l3 = __shfl_up_sync(0xffffffffu, v[3], 1);
+        if (lane == 0) {
+          l2 = Storage<S, T>::load(row[2], sc);
+          l3 = Storage<S, T>::load(row[3], sc);
+        }
+        c[f][r][0] = l2;
+        c[f][r][1] = l3;
+#pragma unroll
+        for (int i = 0; i < 4; ++i) c[f][r][2 + i] = v[i];
+      }
+#pragma unroll
+      for (int r = 0; r < RY; ++r) {
+#pragma unroll
+        for (int d = 0; d < 2; ++d) {
+          const S* row = (d ? zp : zm) + (f * ROWS + w * RY + 1 + r) * RW;
+          T v[4];
+          QuadSm<S>::get(row + 4 + 4 * lane, sc, v);
+          T l3 = __shfl_up_sync(0xffffffffu, v[3], 1);
+          if (lane == 0) l3 = Storage<S, T>::load(row[3], sc);
+          z[f][d][r][0] = l3;
+#pragma unroll
+          for (int i = 0; i < 3; ++i) z[f][d][r][1 + i] = v[i];
+        }
+      }
+    }
+    T out[NF][RY][4];
+    static_for(std::make_integer_sequence<int, RY>{}, [&](auto rc) {
+      constexpr int R = decltype(rc)::value;
+      static_for(std::make_integer_sequence<int, 4>{}, [&](auto ec) {
+        constexpr int E = decltype(ec)::value;
+        QuadAccess<T, NF, RY, R, E> acc{c, z, out};
+        eval<M, Stage>(acc, U);
+      });
+    });
+    if (active) {
+      const int pd = p + 1 < n0 ? p + 1 : 0;   // rolled by one point
+#pragma unroll
+      for (int r = 0; r < RY; ++r) {
+        if (yt + r >= n1) break;
+        const int yd = yt + r + 1 < n1 ? yt + r + 1 : 0;
+#pragma unroll
+        for (int f = 0; f < NF; ++f)
+          Quad<S>::put(static_cast<S*>(L.out[f]) + ((uint32_t)pd * (uint32_t)n1 + (uint32_t)yd) * (uint32_t)n2 + x0,
+                       out[f][r], L.inv_scale[f]);
+      }
+    }
+  }
+  cp_async_wait<0>();   // no copy may land after the block's shared memory is released
+}
+
+template <class Prog, int P, class Stage, int RY, int BW, int PF>
+struct Zring3dVariant {
+  using M = typename Precision<P>::M;
+  using S = typename Precision<P>::S;
+  using Lay = ZringLayout<S, Prog::kFields, RY, BW, PF>;
+  static cudaError_t launch(const FgbLaunch* L, cudaStream_t stream) {
+    auto kern = zring3d_kernel<M, S, Stage, Prog::kFields, RY, BW, PF>;
+    static int resident = 0;   // CTAs of this kernel the device holds at once
+    if (resident == 0) {
+      cudaError_t e = cudaFuncSetAttribute(kern, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)Lay::kBytes);
+      int dev = 0, sms = 0, per_sm = 0;
+      if (e == cudaSuccess) e = cudaGetDevice(&dev);
+      if (e == cudaSuccess) e = cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+      if (e == cudaSuccess) e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * BW, Lay::kBytes);
+      if (e != cudaSuccess) return e;
+      resident = sms * per_sm > 0 ? sms * per_sm : 1;
+    }
+    const int gx = (L->n[2] + 127) / 128, gy = (L->n[1] + BW * RY - 1) / (BW * RY);
+    // at most one wave of CTAs, each walking a chunk of at least 8 planes
+    const int want = resident / (gx * gy) > 1 ? resident / (gx * gy) : 1;
+    const int most = L->n[0] / 8 > 1 ? L->n[0] / 8 : 1;
+    const int gz = want < most ? want : most;
+    kern<<<dim3(gx, gy, gz), dim3(32, BW), Lay::kBytes, stream>>>(*L);
+    return cudaGetLastError();
+  }
+  static FgbFusedVariant describe() {
+    FgbFusedVariant v;
+    v.x_multiple = 4;
+    v.launch = &launch;
+    v.tile_x = 128;
+    v.tile_y = BW * RY;
+    v.steps = 1;
+    v.smem_bytes = Lay::kBytes;
     return v;
   }
 };

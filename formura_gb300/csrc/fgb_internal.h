@@ -34,7 +34,7 @@ struct FgbLaunch {
 #define FGB_TMA_BOX3_Y 32
 #define FGB_TMA_MAP_BYTES 128
 
-#define FGB_MAX_FUSED 8
+#define FGB_MAX_FUSED 12
 
 typedef cudaError_t (*FgbStageLaunch)(const FgbLaunch* args, cudaStream_t stream);
 

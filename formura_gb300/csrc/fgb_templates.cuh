@@ -191,24 +191,105 @@ struct F64Exact {
     return divu_outside(x, c, rc);
 #endif
   }
-  // x normal below the window (exponent under -960), quotient exponent at
-  // least -1000, c in [2^-100, 2^100]
-  static __device__ __forceinline__ bool divu_scaled(T x, T c) {
-    const unsigned ex = expo(x);
-    return within(c, 100) && ex - 1u < 62u && ex + 1000u >= expo(c);
-  }
-  // A warp with a numerator outside the window (a field decaying through
-  // tiny values).  Normal numerators below the window whose quotient is
-  // normal are scaled by 2^256 into it and the quotient scaled back, both
-  // exactly, for five FP64 instructions instead of the IEEE division's ten;
-  // the rest take the IEEE division.  Out of line, so that the compiler
-  // cannot fold its extra products into the common path.
-  static __device__ __noinline__ T divu_outside(T x, T c, T rc) {
-    const bool scaled = divu_scaled(x, c);
-    if (warp_all(divu_window(x, c) || scaled)) {
-      const T q = markstein(__dmul_rn(x, scaled ? 0x1p256 : 1.0), c, rc);
-      return __dmul_rn(q, scaled ? 0x1p-256 : 1.0);
+  // Numerators below the window (a field decaying through tiny values).
+  // Two integer-pipe forms keep them at the window's cost, two FP64
+  // instructions per quotient:
+  //  - x/c of at least 2^-1022: x * 2^256 lies in the window, and the
+  //    quotient comes back by 2^-256 exactly.  That holds when x's exponent
+  //    (a subnormal's counted from its leading bit) is at least c's minus
+  //    1021.
+  //  - x/c below that: its rounding is N * 2^-1074 with N = RN(X / c) an
+  //    integer, X = x * 2^1074 (an integer too).  With q0 = RN(X * RN(1/c))
+  //    below 2^52, q0 is within 1 of X/c, so M, q0 rounded to an integer, is
+  //    within 1.5 and N is M or a neighbour; the exact remainder
+  //    r = X - M*c decides, as in round_quotient, against |c| / 2 (ties to
+  //    even).  X is a multiple of ulp(c) when c <= 2^50, so r is exact
+  //    whenever |r| < |c|.  Below 2^53 the bit pattern of N * 2^-1074 is N
+  //    itself, subnormal or not.
+  // A warp with any other lane takes the IEEE division.
+  //
+  // x * 2^k on the integer pipe for a nonzero x whose exponent field stays
+  // within range: the field moves up by k; a subnormal's significand is
+  // first shifted to its leading bit.
+  template <int K>
+  static __device__ __forceinline__ T scale_up(T x) {
+    unsigned lo, hi;
+    halves(x, lo, hi);
+    const unsigned ex = (hi >> 20) & 0x7ffu;
+    unsigned long long b = ((unsigned long long)hi << 32) | lo;
+    if (ex != 0u) {
+      b += (unsigned long long)K << 52;
+    } else {
+      const unsigned long long m = b & 0x000fffffffffffffull;
+      const int sh = __clzll((long long)m) - 11;
+      b = (b & 0x8000000000000000ull) | ((unsigned long long)(K + 1 - sh) << 52) |
+          ((m << sh) & 0x000fffffffffffffull);
     }
+    return join((unsigned)b, (unsigned)(b >> 32));
+  }
+  // q * 2^-256 for a q whose exponent field exceeds 256: exact
+  static __device__ __forceinline__ T scale_down(T q) {
+    unsigned lo, hi;
+    halves(q, lo, hi);
+    return join(lo, hi - (256u << 20));
+  }
+  // q0 rounded to the nearest integer (halves away from zero), for
+  // |q0| < 2^52: as a double with q0's sign, and its magnitude as an integer
+  static __device__ __forceinline__ T round_integer(T q0, unsigned long long& mi) {
+    unsigned lo, hi;
+    halves(q0, lo, hi);
+    const int e = (int)((hi >> 20) & 0x7ffu) - 1023;
+    unsigned long long b = ((unsigned long long)(hi & 0x7fffffffu) << 32) | lo;
+    if (e < -1) {
+      mi = 0;
+      b = 0;
+    } else if (e == -1) {
+      mi = 1;
+      b = 1023ull << 52;
+    } else {
+      const int f = 52 - e;   // fraction bits, 1 .. 52
+      const unsigned long long half = 1ull << (f - 1);
+      mi = (((b & 0x000fffffffffffffull) | (1ull << 52)) + half) >> f;
+      b = (b + half) & ~((half << 1) - 1ull);
+    }
+    return join((unsigned)b, (unsigned)(b >> 32) | (hi & 0x80000000u));
+  }
+  static __device__ __noinline__ T divu_outside(T x, T c, T rc) {
+    unsigned xlo, xhi, clo, chi;
+    halves(x, xlo, xhi);
+    halves(c, clo, chi);
+    const unsigned ex = (xhi >> 20) & 0x7ffu, ec = (chi >> 20) & 0x7ffu;
+    const unsigned long long mx = ((unsigned long long)(xhi & 0xfffffu) << 32) | xlo;
+    const int eff = ex != 0u ? (int)ex : 12 - __clzll((long long)mx);   // a subnormal's leading bit
+    const bool win = divu_window(x, c);
+    const bool below = !win && within(c, 100) && ex < 63u && mx + ex != 0ull;
+    const bool tiny = below && eff + 1021 >= (int)ec;
+    const bool sub = below && !tiny && ec <= 1073u;
+    if (!warp_all(win || tiny || sub)) return __ddiv_rn(x, c);
+    const T xs = tiny ? scale_up<256>(x) : (sub ? scale_up<1074>(x) : x);
+    const T q0 = __dmul_rn(xs, rc);
+    unsigned long long mi = 0;
+    const T m = sub ? round_integer(q0, mi) : q0;
+    const T r = __fma_rn(-m, c, xs);
+    bool fits;
+    T q;
+    if (sub) {
+      unsigned qlo, qhi, rlo, rhi;
+      halves(q0, qlo, qhi);
+      halves(r, rlo, rhi);
+      fits = ((qhi >> 20) & 0x7ffu) < 1023u + 52u;   // |q0| < 2^52
+      const unsigned long long t = ((unsigned long long)(chi & 0x7fffffffu) << 32 | clo) - (1ull << 52);   // |c|/2
+      const unsigned long long a = ((unsigned long long)(rhi & 0x7fffffffu) << 32) | rlo;
+      const bool step = a > t || (a == t && (mi & 1ull));
+      const bool up = ((rhi ^ xhi) >> 31) == 0;   // X/c lies above M
+      const unsigned long long n = mi + (step ? (up ? 1ull : ~0ull) : 0ull);
+      const unsigned long long sgn = (unsigned long long)((xhi ^ chi) >> 31) << 63;
+      q = join((unsigned)n, (unsigned)((sgn | n) >> 32));
+    } else {
+      q = round_quotient(xs, c, q0, r, fits);
+      if (tiny) q = scale_down(q);
+    }
+    if (warp_all(fits)) return q;
     return __ddiv_rn(x, c);
   }
   // RN(1/b) for a grid value b that several quotients divide by
@@ -528,7 +609,8 @@ __global__ void __launch_bounds__(kBlockX) adjoint_kernel(const __grid_constant_
 
 // rows per thread: several for the memory-bound FP32/FP16 forms (four for
 // single-kernel steps, two for the larger stages of multi-stage programs),
-// one for FP64, which is bound by the FP64 pipe
+// one for FP64, which is bound by the FP64 pipe (two or four rows gave
+// Gray-Scott the same 17.2 GLUP/s)
 template <int P, bool Light>
 constexpr int rows_per_thread() { return P >= 2 ? (Light ? 4 : 2) : 1; }
 
@@ -616,6 +698,11 @@ struct FusedFill {
       if constexpr ((P == 2 || P == 3) && Prog::kStar && Prog::kReach == 1 && Prog::kShift == 1) {
         d.fused[P][count++] = Quad3dVariant<Prog, P, Stage0, 2, 4>::describe();
         d.fused[P][count++] = Quad3dVariant<Prog, P, Stage0, 4, 2>::describe();
+        // the same vectors, a chunk of planes per CTA through a shared-memory ring
+        d.fused[P][count++] = Zring3dVariant<Prog, P, Stage0, 2, 4, 3>::describe();
+        d.fused[P][count++] = Zring3dVariant<Prog, P, Stage0, 2, 8, 3>::describe();
+        d.fused[P][count++] = Zring3dVariant<Prog, P, Stage0, 1, 8, 4>::describe();
+        d.fused[P][count++] = Zring3dVariant<Prog, P, Stage0, 4, 4, 2>::describe();
       }
       d.nfused[P] = count;
       d.nbatch[P] = 0;

@@ -11,7 +11,11 @@
  * is not a quotient of two doubles), exact quotients, and quotients within
  * a few ulps of a power of two, where the form does not apply (there the
  * neighbours below are half as far apart).
- * Prints "mismatches applied not_applied". */
+ * Numerators below the window (subnormal ones included) take the device's
+ * two integer-pipe forms: scaled by 2^256 and the quotient scaled back where
+ * it is normal, rounded on the grid of 2^-1074 where it is not.
+ * Prints "mismatches applied not_applied outside_mismatches scaled_cases
+ * subnormal_quotient_cases". */
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -40,6 +44,95 @@ static double round_quotient(double x, double c, double q0, double r, int* fits)
   const int up = ((rhi ^ chi ^ qhi) >> 31) == 0;
   const uint64_t res = qb + (step ? (up ? 1ull : ~0ull) : 0ull);
   return zero ? q0 : from(res);
+}
+
+/* the device's path for numerators below the window (F64Exact::divu_outside),
+   step for step: x * 2^256 on the integer pipe and the quotient scaled back
+   where x/c is at least 2^-1022; below that N = RN(X / c) for the integer
+   X = x * 2^1074, from M = q0 rounded to an integer and the exact remainder
+   X - M*c, and the bit pattern N.  Returns 0 where the device would take the
+   IEEE division instead. */
+static int window(double x, double c) {
+  const unsigned ex = (unsigned)(bits(x) >> 52) & 0x7ffu, ec = (unsigned)(bits(c) >> 52) & 0x7ffu;
+  const int zero = (bits(x) << 1) == 0;
+  return ec - 923u <= 200u && (zero || (ex - 63u <= 1920u && ex - ec + 1000u <= 2000u));
+}
+static double scale_up(double x, int k) {
+  uint64_t b = bits(x);
+  const unsigned ex = (unsigned)(b >> 52) & 0x7ffu;
+  if (ex != 0u) {
+    b += (uint64_t)k << 52;
+  } else {
+    const uint64_t m = b & 0x000fffffffffffffull;
+    const int sh = __builtin_clzll(m) - 11;
+    b = (b & 0x8000000000000000ull) | ((uint64_t)(k + 1 - sh) << 52) | ((m << sh) & 0x000fffffffffffffull);
+  }
+  return from(b);
+}
+static double round_integer(double q0, uint64_t* mi) {
+  const uint64_t qb = bits(q0);
+  const int e = (int)((qb >> 52) & 0x7ff) - 1023;
+  uint64_t b = qb & 0x7fffffffffffffffull;
+  if (e < -1) {
+    *mi = 0;
+    b = 0;
+  } else if (e == -1) {
+    *mi = 1;
+    b = 1023ull << 52;
+  } else {
+    const int f = 52 - e;
+    const uint64_t half = 1ull << (f - 1);
+    *mi = (((b & 0x000fffffffffffffull) | (1ull << 52)) + half) >> f;
+    b = (b + half) & ~((half << 1) - 1ull);
+  }
+  return from(b | (qb & 0x8000000000000000ull));
+}
+/* 1: tiny path, 2: subnormal-quotient path, 0: IEEE */
+static int outside(double x, double c, double* out) {
+  const uint64_t xb = bits(x), cb = bits(c);
+  const unsigned ex = (unsigned)(xb >> 52) & 0x7ffu, ec = (unsigned)(cb >> 52) & 0x7ffu;
+  const uint64_t mx = xb & 0x000fffffffffffffull;
+  const int eff = ex != 0u ? (int)ex : 12 - __builtin_clzll(mx ? mx : 1);
+  const int win = window(x, c);
+  const int below = !win && ec - 923u <= 200u && ex < 63u && mx + ex != 0ull;
+  const int tiny = below && eff + 1021 >= (int)ec;
+  const int sub = below && !tiny && ec <= 1073u;
+  if (!(tiny || sub)) return 0;
+  const double xs = tiny ? scale_up(x, 256) : scale_up(x, 1074);
+  if (bits(xs) != bits(ldexp(x, tiny ? 256 : 1074))) return -1;   /* the scaling itself is wrong */
+  const double y = 1.0 / c, q0 = xs * y;
+  uint64_t mi = 0;
+  const double m = sub ? round_integer(q0, &mi) : q0;
+  const double r = fma(-m, c, xs);
+  int fits;
+  if (sub) {
+    fits = ((bits(q0) >> 52) & 0x7ffu) < 1023u + 52u;
+    const uint64_t t = (cb & 0x7fffffffffffffffull) - (1ull << 52);
+    const uint64_t a = bits(r) & 0x7fffffffffffffffull;
+    const int step = a > t || (a == t && (mi & 1ull));
+    const int up = ((bits(r) ^ xb) >> 63) == 0;
+    const uint64_t n = mi + (step ? (up ? 1ull : ~0ull) : 0ull);
+    *out = from((((xb ^ cb) >> 63) << 63) | n);
+  } else {
+    double q = round_quotient(xs, c, q0, r, &fits);
+    *out = from(bits(q) - (256ull << 52));
+  }
+  return fits ? (tiny ? 1 : 2) : 0;
+}
+
+static long tiny_bad = 0, tiny_done = 0, sub_done = 0;
+
+static void check_outside(double x, double c) {
+  double q;
+  const int k = outside(x, c, &q);
+  if (k < 0) {
+    ++tiny_bad;
+    return;
+  }
+  if (k == 0) return;
+  tiny_done += k == 1;
+  sub_done += k == 2;
+  tiny_bad += bits(q) != bits(x / c);
 }
 
 static double operand(int lo, int hi) {
@@ -97,9 +190,25 @@ int main(int argc, char** argv) {
       check(nextafter(q * cc, INFINITY), cc);
       check(nextafter(q * cc, -INFINITY), cc);
     }
+    /* numerators below the window: subnormal and the lowest binades, with
+       constants over the window; quotients normal, subnormal or zero */
+    {
+      const double cc = operand(1023 - 100, 1023 + 50);
+      const uint64_t sb = (rnd() & 1) << 63;
+      check_outside(from(sb | ((rnd() & 0x000fffffffffffffull) >> (rnd() % 52))), cc);
+      check_outside(from(sb | ((rnd() % 63) << 52) | (rnd() & 0x000fffffffffffffull)), cc);
+      /* x/c at or next to a midpoint of the subnormal grid: c with a short
+         significand, x = (N + 1/2) * c rounded, and its neighbours */
+      const double cs = from((bits(operand(1023 - 30, 1023 + 20)) & 0xffffff0000000000ull) & 0x7fffffffffffffffull);
+      const double xm = ldexp((double)(rnd() % (1ull << 40)) + 0.5, -1074) * cs;
+      check_outside(xm, cs);
+      check_outside(nextafter(xm, INFINITY), cs);
+      check_outside(nextafter(xm, -INFINITY), cs);
+      check_outside(-xm, cs);
+    }
     /* signed zero numerators */
     if (i % 64 == 0) check(from((rnd() & 1) << 63), operand(1023 - 100, 1023 + 100));
   }
-  printf("%ld %ld %ld\n", bad, applied, skipped);
+  printf("%ld %ld %ld %ld %ld %ld\n", bad, applied, skipped, tiny_bad, tiny_done, sub_done);
   return 0;
 }
