@@ -141,18 +141,19 @@ struct F64Exact {
     halves(q0, qlo, qhi);
     halves(r, rlo, rhi);
     halves(c, clo, chi);
-    const unsigned eq = (qhi >> 20) & 0x7ffu, ec = (chi >> 20) & 0x7ffu;
-    const unsigned long long m = ((unsigned long long)(qhi & 0xfffffu) << 32) | qlo;
-    const int et = (int)ec + (int)eq - 1076;   // exponent field of |c| * ulp(q0) / 2
+    const int et = (int)((chi >> 20) & 0x7ffu) + (int)((qhi >> 20) & 0x7ffu) - 1076;   // of |c| * ulp(q0) / 2
     const bool zero = is_zero(x);
-    fits = zero || (m - 2ull <= (1ull << 52) - 5ull && (unsigned)(et - 2) <= 2044u);
-    const unsigned long long t = ((unsigned long long)((chi & 0xfffffu) | ((unsigned)et << 20)) << 32) | clo;
-    const unsigned long long a = ((unsigned long long)(rhi & 0x7fffffffu) << 32) | rlo;
-    const bool step = a > t || (a == t && (qlo & 1u));
+    // q0's low word away from 0, 1 and its two largest values: then q0 lies
+    // at least two ulps inside its binade, and a neighbour differs from it
+    // in the low word only
+    fits = zero || (qlo - 2u <= 0xfffffffbu && (unsigned)(et - 2) <= 2044u);
+    const unsigned thi = (chi & 0xfffffu) | ((unsigned)et << 20), ahi = rhi & 0x7fffffffu;
+    const bool gt = ahi > thi || (ahi == thi && rlo > clo);
+    const bool tie = ahi == thi && rlo == clo;
+    const bool step = gt || (tie && (qlo & 1u));
     const bool up = ((rhi ^ chi ^ qhi) >> 31) == 0;   // towards x/c the magnitude grows
-    const unsigned long long qb = ((unsigned long long)qhi << 32) | qlo;
-    const unsigned long long res = qb + (step ? (up ? 1ull : ~0ull) : 0ull);
-    return zero ? q0 : join((unsigned)res, (unsigned)(res >> 32));
+    const unsigned lo = qlo + (step ? (up ? 1u : 0xffffffffu) : 0u);
+    return zero ? q0 : join(lo, qhi);
   }
   // RN(x / c) inside Markstein's window: two FP64 instructions and the
   // integer step where it applies to every lane of the warp, else
@@ -192,21 +193,15 @@ struct F64Exact {
 #endif
   }
   // Numerators below the window (a field decaying through tiny values).
-  // Two integer-pipe forms keep them at the window's cost, two FP64
-  // instructions per quotient:
-  //  - x/c of at least 2^-1022: x * 2^256 lies in the window, and the
-  //    quotient comes back by 2^-256 exactly.  That holds when x's exponent
-  //    (a subnormal's counted from its leading bit) is at least c's minus
-  //    1021.
-  //  - x/c below that: its rounding is N * 2^-1074 with N = RN(X / c) an
-  //    integer, X = x * 2^1074 (an integer too).  With q0 = RN(X * RN(1/c))
-  //    below 2^52, q0 is within 1 of X/c, so M, q0 rounded to an integer, is
-  //    within 1.5 and N is M or a neighbour; the exact remainder
-  //    r = X - M*c decides, as in round_quotient, against |c| / 2 (ties to
-  //    even).  X is a multiple of ulp(c) when c <= 2^50, so r is exact
-  //    whenever |r| < |c|.  Below 2^53 the bit pattern of N * 2^-1074 is N
-  //    itself, subnormal or not.
-  // A warp with any other lane takes the IEEE division.
+  // Where x/c is at least 2^-1022, x * 2^256 lies in the window and the
+  // quotient comes back by 2^-256 exactly, both on the integer pipe, so such
+  // a quotient costs what one inside the window costs.  That holds when x's
+  // exponent (a subnormal's counted from its leading bit) is at least c's
+  // minus 1021.  A warp with any other lane (a subnormal quotient, say)
+  // takes the IEEE division: an exact rounding on the subnormal grid with
+  // the integer pipe was built and measured slower (Gray-Scott's decayed
+  // far field, 15.5 GLUP/s against 16.0).  Out of line, so that the compiler
+  // cannot fold this path into the common one.
   //
   // x * 2^k on the integer pipe for a nonzero x whose exponent field stays
   // within range: the field moves up by k; a subnormal's significand is
@@ -233,63 +228,20 @@ struct F64Exact {
     halves(q, lo, hi);
     return join(lo, hi - (256u << 20));
   }
-  // q0 rounded to the nearest integer (halves away from zero), for
-  // |q0| < 2^52: as a double with q0's sign, and its magnitude as an integer
-  static __device__ __forceinline__ T round_integer(T q0, unsigned long long& mi) {
+  static __device__ __forceinline__ bool divu_tiny(T x, T c) {
     unsigned lo, hi;
-    halves(q0, lo, hi);
-    const int e = (int)((hi >> 20) & 0x7ffu) - 1023;
-    unsigned long long b = ((unsigned long long)(hi & 0x7fffffffu) << 32) | lo;
-    if (e < -1) {
-      mi = 0;
-      b = 0;
-    } else if (e == -1) {
-      mi = 1;
-      b = 1023ull << 52;
-    } else {
-      const int f = 52 - e;   // fraction bits, 1 .. 52
-      const unsigned long long half = 1ull << (f - 1);
-      mi = (((b & 0x000fffffffffffffull) | (1ull << 52)) + half) >> f;
-      b = (b + half) & ~((half << 1) - 1ull);
-    }
-    return join((unsigned)b, (unsigned)(b >> 32) | (hi & 0x80000000u));
+    halves(x, lo, hi);
+    const unsigned ex = (hi >> 20) & 0x7ffu;
+    const unsigned long long m = ((unsigned long long)(hi & 0xfffffu) << 32) | lo;
+    const int eff = ex != 0u ? (int)ex : 12 - __clzll((long long)m);   // a subnormal's leading bit
+    return within(c, 100) && ex < 63u && m + ex != 0ull && eff + 1021 >= (int)expo(c);
   }
   static __device__ __noinline__ T divu_outside(T x, T c, T rc) {
-    unsigned xlo, xhi, clo, chi;
-    halves(x, xlo, xhi);
-    halves(c, clo, chi);
-    const unsigned ex = (xhi >> 20) & 0x7ffu, ec = (chi >> 20) & 0x7ffu;
-    const unsigned long long mx = ((unsigned long long)(xhi & 0xfffffu) << 32) | xlo;
-    const int eff = ex != 0u ? (int)ex : 12 - __clzll((long long)mx);   // a subnormal's leading bit
-    const bool win = divu_window(x, c);
-    const bool below = !win && within(c, 100) && ex < 63u && mx + ex != 0ull;
-    const bool tiny = below && eff + 1021 >= (int)ec;
-    const bool sub = below && !tiny && ec <= 1073u;
-    if (!warp_all(win || tiny || sub)) return __ddiv_rn(x, c);
-    const T xs = tiny ? scale_up<256>(x) : (sub ? scale_up<1074>(x) : x);
-    const T q0 = __dmul_rn(xs, rc);
-    unsigned long long mi = 0;
-    const T m = sub ? round_integer(q0, mi) : q0;
-    const T r = __fma_rn(-m, c, xs);
-    bool fits;
-    T q;
-    if (sub) {
-      unsigned qlo, qhi, rlo, rhi;
-      halves(q0, qlo, qhi);
-      halves(r, rlo, rhi);
-      fits = ((qhi >> 20) & 0x7ffu) < 1023u + 52u;   // |q0| < 2^52
-      const unsigned long long t = ((unsigned long long)(chi & 0x7fffffffu) << 32 | clo) - (1ull << 52);   // |c|/2
-      const unsigned long long a = ((unsigned long long)(rhi & 0x7fffffffu) << 32) | rlo;
-      const bool step = a > t || (a == t && (mi & 1ull));
-      const bool up = ((rhi ^ xhi) >> 31) == 0;   // X/c lies above M
-      const unsigned long long n = mi + (step ? (up ? 1ull : ~0ull) : 0ull);
-      const unsigned long long sgn = (unsigned long long)((xhi ^ chi) >> 31) << 63;
-      q = join((unsigned)n, (unsigned)((sgn | n) >> 32));
-    } else {
-      q = round_quotient(xs, c, q0, r, fits);
-      if (tiny) q = scale_down(q);
+    const bool tiny = divu_tiny(x, c);
+    if (warp_all(divu_window(x, c) || tiny)) {
+      const T q = quotient(tiny ? scale_up<256>(x) : x, c, rc);
+      return tiny ? scale_down(q) : q;
     }
-    if (warp_all(fits)) return q;
     return __ddiv_rn(x, c);
   }
   // RN(1/b) for a grid value b that several quotients divide by

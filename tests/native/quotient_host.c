@@ -1,7 +1,8 @@
 /* Host check of the bit-faithful FP64 policy's quotient with its last
  * rounding step on the integer pipe (fgb::F64Exact::round_quotient):
  * y = RN(1/c), q0 = RN(x*y), r = x - q0*c (one fma, exact), and then, where
- * q0 lies at least two ulps inside its binade, RN(x/c) is q0 or the
+ * q0's low word is away from its extremes (so q0 lies at least two ulps
+ * inside its binade), RN(x/c) is q0 or the
  * neighbour towards x/c: the neighbour when |r| > |c| * ulp(q0) / 2, the
  * even one of the two when |r| equals it.  The same integer steps as the
  * device code, on the host's correctly rounded fma; compared with the
@@ -11,11 +12,10 @@
  * is not a quotient of two doubles), exact quotients, and quotients within
  * a few ulps of a power of two, where the form does not apply (there the
  * neighbours below are half as far apart).
- * Numerators below the window (subnormal ones included) take the device's
- * two integer-pipe forms: scaled by 2^256 and the quotient scaled back where
- * it is normal, rounded on the grid of 2^-1074 where it is not.
- * Prints "mismatches applied not_applied outside_mismatches scaled_cases
- * subnormal_quotient_cases". */
+ * Numerators below the window (subnormal ones included) whose quotient is
+ * normal are scaled by 2^256 on the integer pipe first and the quotient
+ * scaled back, as on the device.
+ * Prints "mismatches applied not_applied tiny_mismatches tiny_cases". */
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -33,30 +33,22 @@ static double round_quotient(double x, double c, double q0, double r, int* fits)
   const unsigned qhi = (unsigned)(qb >> 32), qlo = (unsigned)qb;
   const unsigned rhi = (unsigned)(rb >> 32), rlo = (unsigned)rb;
   const unsigned chi = (unsigned)(cb >> 32), clo = (unsigned)cb;
-  const unsigned eq = (qhi >> 20) & 0x7ffu, ec = (chi >> 20) & 0x7ffu;
-  const uint64_t m = ((uint64_t)(qhi & 0xfffffu) << 32) | qlo;
-  const int et = (int)ec + (int)eq - 1076;
+  const int et = (int)((chi >> 20) & 0x7ffu) + (int)((qhi >> 20) & 0x7ffu) - 1076;
   const int zero = ((bits(x) << 1) == 0);
-  *fits = zero || ((m - 2u <= (1ull << 52) - 5u) && (unsigned)(et - 2) <= 2044u);
-  const uint64_t t = ((uint64_t)((chi & 0xfffffu) | ((unsigned)et << 20)) << 32) | clo;
-  const uint64_t a = ((uint64_t)(rhi & 0x7fffffffu) << 32) | rlo;
-  const int step = a > t || (a == t && (qlo & 1u));
+  *fits = zero || (qlo - 2u <= 0xfffffffbu && (unsigned)(et - 2) <= 2044u);
+  const unsigned thi = (chi & 0xfffffu) | ((unsigned)et << 20), ahi = rhi & 0x7fffffffu;
+  const int gt = ahi > thi || (ahi == thi && rlo > clo);
+  const int tie = ahi == thi && rlo == clo;
+  const int step = gt || (tie && (qlo & 1u));
   const int up = ((rhi ^ chi ^ qhi) >> 31) == 0;
-  const uint64_t res = qb + (step ? (up ? 1ull : ~0ull) : 0ull);
-  return zero ? q0 : from(res);
+  const unsigned lo = qlo + (step ? (up ? 1u : 0xffffffffu) : 0u);
+  return zero ? q0 : from(((uint64_t)qhi << 32) | lo);
 }
 
 /* the device's path for numerators below the window (F64Exact::divu_outside),
-   step for step: x * 2^256 on the integer pipe and the quotient scaled back
-   where x/c is at least 2^-1022; below that N = RN(X / c) for the integer
-   X = x * 2^1074, from M = q0 rounded to an integer and the exact remainder
-   X - M*c, and the bit pattern N.  Returns 0 where the device would take the
-   IEEE division instead. */
-static int window(double x, double c) {
-  const unsigned ex = (unsigned)(bits(x) >> 52) & 0x7ffu, ec = (unsigned)(bits(c) >> 52) & 0x7ffu;
-  const int zero = (bits(x) << 1) == 0;
-  return ec - 923u <= 200u && (zero || (ex - 63u <= 1920u && ex - ec + 1000u <= 2000u));
-}
+   step for step: where x/c is at least 2^-1022, x * 2^256 on the integer
+   pipe, the quotient, and the quotient scaled back.  Returns 0 where the
+   device would take the IEEE division instead. */
 static double scale_up(double x, int k) {
   uint64_t b = bits(x);
   const unsigned ex = (unsigned)(b >> 52) & 0x7ffu;
@@ -69,58 +61,23 @@ static double scale_up(double x, int k) {
   }
   return from(b);
 }
-static double round_integer(double q0, uint64_t* mi) {
-  const uint64_t qb = bits(q0);
-  const int e = (int)((qb >> 52) & 0x7ff) - 1023;
-  uint64_t b = qb & 0x7fffffffffffffffull;
-  if (e < -1) {
-    *mi = 0;
-    b = 0;
-  } else if (e == -1) {
-    *mi = 1;
-    b = 1023ull << 52;
-  } else {
-    const int f = 52 - e;
-    const uint64_t half = 1ull << (f - 1);
-    *mi = (((b & 0x000fffffffffffffull) | (1ull << 52)) + half) >> f;
-    b = (b + half) & ~((half << 1) - 1ull);
-  }
-  return from(b | (qb & 0x8000000000000000ull));
-}
-/* 1: tiny path, 2: subnormal-quotient path, 0: IEEE */
 static int outside(double x, double c, double* out) {
   const uint64_t xb = bits(x), cb = bits(c);
   const unsigned ex = (unsigned)(xb >> 52) & 0x7ffu, ec = (unsigned)(cb >> 52) & 0x7ffu;
   const uint64_t mx = xb & 0x000fffffffffffffull;
   const int eff = ex != 0u ? (int)ex : 12 - __builtin_clzll(mx ? mx : 1);
-  const int win = window(x, c);
-  const int below = !win && ec - 923u <= 200u && ex < 63u && mx + ex != 0ull;
-  const int tiny = below && eff + 1021 >= (int)ec;
-  const int sub = below && !tiny && ec <= 1073u;
-  if (!(tiny || sub)) return 0;
-  const double xs = tiny ? scale_up(x, 256) : scale_up(x, 1074);
-  if (bits(xs) != bits(ldexp(x, tiny ? 256 : 1074))) return -1;   /* the scaling itself is wrong */
-  const double y = 1.0 / c, q0 = xs * y;
-  uint64_t mi = 0;
-  const double m = sub ? round_integer(q0, &mi) : q0;
-  const double r = fma(-m, c, xs);
+  if (!(ec - 923u <= 200u && ex < 63u && mx + ex != 0ull && eff + 1021 >= (int)ec)) return 0;
+  const double xs = scale_up(x, 256);
+  if (bits(xs) != bits(ldexp(x, 256))) return -1;   /* the scaling itself is wrong */
+  const double y = 1.0 / c, q0 = xs * y, r = fma(-q0, c, xs);
   int fits;
-  if (sub) {
-    fits = ((bits(q0) >> 52) & 0x7ffu) < 1023u + 52u;
-    const uint64_t t = (cb & 0x7fffffffffffffffull) - (1ull << 52);
-    const uint64_t a = bits(r) & 0x7fffffffffffffffull;
-    const int step = a > t || (a == t && (mi & 1ull));
-    const int up = ((bits(r) ^ xb) >> 63) == 0;
-    const uint64_t n = mi + (step ? (up ? 1ull : ~0ull) : 0ull);
-    *out = from((((xb ^ cb) >> 63) << 63) | n);
-  } else {
-    double q = round_quotient(xs, c, q0, r, &fits);
-    *out = from(bits(q) - (256ull << 52));
-  }
-  return fits ? (tiny ? 1 : 2) : 0;
+  double q = round_quotient(xs, c, q0, r, &fits);
+  if (!fits) q = fma(r, y, q0);
+  *out = from(bits(q) - (256ull << 52));
+  return 1;
 }
 
-static long tiny_bad = 0, tiny_done = 0, sub_done = 0;
+static long tiny_bad = 0, tiny_done = 0;
 
 static void check_outside(double x, double c) {
   double q;
@@ -130,8 +87,7 @@ static void check_outside(double x, double c) {
     return;
   }
   if (k == 0) return;
-  tiny_done += k == 1;
-  sub_done += k == 2;
+  ++tiny_done;
   tiny_bad += bits(q) != bits(x / c);
 }
 
@@ -190,25 +146,16 @@ int main(int argc, char** argv) {
       check(nextafter(q * cc, INFINITY), cc);
       check(nextafter(q * cc, -INFINITY), cc);
     }
-    /* numerators below the window: subnormal and the lowest binades, with
-       constants over the window; quotients normal, subnormal or zero */
+    /* numerators below the window: subnormal and the lowest binades */
     {
-      const double cc = operand(1023 - 100, 1023 + 50);
+      const double cc = operand(1023 - 100, 1023 + 100);
       const uint64_t sb = (rnd() & 1) << 63;
       check_outside(from(sb | ((rnd() & 0x000fffffffffffffull) >> (rnd() % 52))), cc);
       check_outside(from(sb | ((rnd() % 63) << 52) | (rnd() & 0x000fffffffffffffull)), cc);
-      /* x/c at or next to a midpoint of the subnormal grid: c with a short
-         significand, x = (N + 1/2) * c rounded, and its neighbours */
-      const double cs = from((bits(operand(1023 - 30, 1023 + 20)) & 0xffffff0000000000ull) & 0x7fffffffffffffffull);
-      const double xm = ldexp((double)(rnd() % (1ull << 40)) + 0.5, -1074) * cs;
-      check_outside(xm, cs);
-      check_outside(nextafter(xm, INFINITY), cs);
-      check_outside(nextafter(xm, -INFINITY), cs);
-      check_outside(-xm, cs);
     }
     /* signed zero numerators */
     if (i % 64 == 0) check(from((rnd() & 1) << 63), operand(1023 - 100, 1023 + 100));
   }
-  printf("%ld %ld %ld %ld %ld %ld\n", bad, applied, skipped, tiny_bad, tiny_done, sub_done);
+  printf("%ld %ld %ld %ld %ld\n", bad, applied, skipped, tiny_bad, tiny_done);
   return 0;
 }
