@@ -386,6 +386,51 @@ def time_grid(grid, spf, warmup, steps, torch, stream, flush=None, reset=None):
 BOUNDS = {"f64fast": 1e-12, "f32": 1e-5, "f16": 1e-5}
 
 
+def run_sweep(args, spec):
+    """Every kernel the autotuner chooses among for this workload, size and
+    precision (the generic stage kernels, index -1, and each fused variant),
+    timed on its own with CUDA events over --steps bench steps of --spf time
+    steps after --warmup, from the workload's initial state: one JSON line
+    per kernel.  A measurement aid; the bench line itself keeps the
+    autotuner's choice."""
+    import numpy as np
+    import torch
+    from formura_gb300 import build as B
+    if not os.path.exists(B.LIB):
+        B.build()
+    from formura_gb300.host import FormuraProgram, Grid, builtin_program, program_uniforms
+    src, _ = builtin_program(spec["program"])
+    cells = 1
+    for x in spec["shape"]:
+        cells *= x
+    dp = FormuraProgram(src, spec["cfg"] + "gpu_steps_per_forward: 1\ngpu_autotune: 0\n", spec["program"],
+                        name=f"{spec['program']}_sweep")
+    dp.init()
+    st0 = initial_state(spec, dp)
+    _, U = program_uniforms(src, spec["cfg"], spec["program"])
+    sc = None
+    if args.precision == "f16":
+        sc = [float(max(1e-3, np.abs(st0[i]).max())) for i in range(spec["fields"])]
+    g = Grid(spec["program"], spec["shape"], args.precision, U, scales=sc)
+    stream = torch.cuda.ExternalStream(g.stream)
+    for v in [-1] + [v["index"] for v in g.variants()]:
+        g.upload(st0)
+        try:
+            g.set_variant(v)
+        except Exception as e:   # does not fit this grid or this device
+            print(json.dumps({"sweep": spec["label"], "variant": v, "skipped": str(e)[:120]}), flush=True)
+            continue
+        ms, launches = time_grid(g, args.spf, args.warmup, args.steps, torch, stream, None,
+                                 lambda grid: grid.upload(st0))
+        tsteps = args.steps * args.spf
+        kernel = g.variants()[v] if v >= 0 else "generic stage kernels"
+        print(json.dumps({"sweep": spec["label"], "precision": args.precision, "variant": v, "kernel": kernel,
+                          "value": cells * tsteps / (ms / 1e3) / 1e9, "unit": "GLUP/s",
+                          "ms_per_time_step": ms / tsteps, "time_steps": tsteps, "launches": launches}),
+              flush=True)
+    g.close()
+
+
 def run_ours(args, spec):
     import numpy as np
     import torch
@@ -609,6 +654,8 @@ def main():
     ap.add_argument("--no-autotune", action="store_true")
     ap.add_argument("--variant", type=int, default=None, help="use this temporal-blocking kernel (no autotune)")
     ap.add_argument("--size", type=int, default=None, help="grid points per axis (smaller profiling cases)")
+    ap.add_argument("--sweep", action="store_true",
+                    help="time every kernel the autotuner chooses among, one JSON line each, and exit")
     ap.add_argument("--adj-n", type=int, default=512)
     ap.add_argument("--adj-steps", type=int, default=200)
     ap.add_argument("--probes", type=int, default=64)
@@ -636,7 +683,9 @@ def main():
         args.spf = spec["spf"]
     if args.steps is None:
         args.steps = max(1, spec["steps_total"] // args.spf)
-    if args.impl == "reference":
+    if args.sweep:
+        run_sweep(args, spec)
+    elif args.impl == "reference":
         run_reference(args, spec)
     else:
         run_ours(args, spec)
