@@ -341,12 +341,13 @@ def storage_bytes(precision):
 L2_BYTES = 129 * 2**20
 
 
-def time_grid(grid, spf, warmup, steps, torch, stream, flush=None, reset=None):
+def time_grid(grid, spf, warmup, steps, torch, stream, flush=None, reset=None, per_step=None):
     """Device time of `steps` bench steps of `spf` time steps each, after
     `warmup` untimed bench steps and `reset()` (back to the initial state, so
     that the timed steps cover time steps 0 .. steps*spf of the workload).
     With a flush buffer (states that fit in L2) every bench step is timed on
-    its own after the buffer was overwritten, and the times are summed."""
+    its own after the buffer was overwritten, and the times are summed.
+    `per_step`, a list, receives each bench step's time."""
     for _ in range(warmup):
         grid.forward(spf)
     grid.synchronize()
@@ -356,15 +357,16 @@ def time_grid(grid, spf, warmup, steps, torch, stream, flush=None, reset=None):
     l0 = grid.launches
     torch.cuda.synchronize()
     if flush is None:
-        ev0 = torch.cuda.Event(enable_timing=True)
-        ev1 = torch.cuda.Event(enable_timing=True)
-        ev0.record(stream)
-        for _ in range(steps):
+        evs = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+        evs[0].record(stream)
+        for i in range(steps):
             grid.forward(spf)
-        ev1.record(stream)
-        ev1.synchronize()
+            evs[i + 1].record(stream)
+        evs[-1].synchronize()
         torch.cuda.synchronize()
-        return ev0.elapsed_time(ev1), grid.launches - l0
+        if per_step is not None:
+            per_step.extend(evs[i].elapsed_time(evs[i + 1]) for i in range(steps))
+        return evs[0].elapsed_time(evs[-1]), grid.launches - l0
     evs = []
     with torch.cuda.stream(stream):
         for _ in range(steps):
@@ -376,6 +378,8 @@ def time_grid(grid, spf, warmup, steps, torch, stream, flush=None, reset=None):
             e1.record(stream)
             evs.append((e0, e1))
     torch.cuda.synchronize()
+    if per_step is not None:
+        per_step.extend(a.elapsed_time(b) for a, b in evs)
     return sum(a.elapsed_time(b) for a, b in evs), grid.launches - l0
 
 
@@ -494,7 +498,8 @@ def run_ours(args, spec):
         return flush_buf[0]
 
     flush = flush_for(args.precision)
-    ms, launches = time_grid(g, spf, args.warmup, args.steps, torch, stream, flush, reset)
+    step_ms = []
+    ms, launches = time_grid(g, spf, args.warmup, args.steps, torch, stream, flush, reset, step_ms)
     clocks = sampler.stop()
     ms = max_over_ranks(ms, ws, "cuda")
     final64 = g.download()
@@ -552,11 +557,23 @@ def run_ours(args, spec):
     # the initial state and the calls are timed one by one.  Between calls
     # (untimed) every reduced-precision grid advances the same steps from the
     # same state, and its distance to the drop-in's FP64 formura_data is
-    # recorded: the error of each form along the whole horizon.
+    # recorded: the error of each form along the whole horizon.  A line of
+    # another precision times a drop-in built with that precision
+    # (gpu_precision, and its kernel chosen at Formura_Init as here).
+    de = dp
+    if args.precision != "f64":
+        extra = (f"gpu_steps_per_forward: {spf}\ngpu_precision: {args.precision}\n"
+                 f"gpu_autotune: {0 if args.no_autotune else 1}\n")
+        if args.precision == "f16":
+            extra += "gpu_field_scales: [" + ", ".join(
+                repr(float(max(1e-3, np.abs(st0[i]).max()))) for i in range(nf)) + "]\n"
+        de = FormuraProgram(src, spec["cfg"] + extra, spec["program"],
+                            name=f"{spec['program']}_bench_e2e_{args.precision}_{local}")
+        de.init()
     for _ in range(2):
-        dp.forward(1)
-    for i, f in enumerate(dp.fields):
-        dp.set(f, st0[i])
+        de.forward(1)
+    for i, f in enumerate(de.fields):
+        de.set(f, st0[i])
     for gv in vgrids.values():
         reset(gv)
     track = {p: [] for p in vgrids}
@@ -567,7 +584,7 @@ def run_ours(args, spec):
     call_ms = []
     for c in range(e2e_calls):
         t0 = time.perf_counter()
-        dp.forward(1)
+        de.forward(1)
         call_ms.append((time.perf_counter() - t0) * 1e3)
         e2e_s += call_ms[-1] / 1e3
         if vgrids:
@@ -579,7 +596,7 @@ def run_ours(args, spec):
     e2e = {"value": ws * cells * e2e_calls * spf / e2e_s / 1e9, "unit": "GLUP/s",
            "h2d_bytes_per_step": nf * cells * 8, "d2h_bytes_per_step": nf * cells * 8,
            "steps": e2e_calls, "time_steps": e2e_calls * spf,
-           "api": "Formura_Forward (drop-in C API, formura_data on the host)",
+           "api": f"Formura_Forward (drop-in C API, formura_data on the host, gpu_precision {args.precision})",
            "call_ms": [round(x, 2) for x in call_ms],
            "clocks": e2e_sampler.stop()}
     for p, gv in vgrids.items():
@@ -606,7 +623,8 @@ def run_ours(args, spec):
                                   "overwritten before every timed bench step") %
                                  (nf * cells * storage_bytes(args.precision) // 2**20),
                            "parallelism": "replicas" if ws > 1 else "single GPU"},
-                "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clocks}
+                "roofline": roofline, "e2e": e2e, "gpu_launches": launches, "clocks": clocks,
+                "bench_step_ms": [round(x, 3) for x in step_ms]}
         fp64 = fp64_pipe(spec, args.precision, value / ws, dfma_rate())
         if fp64 is not None:
             line["fp64_pipe_bound"] = fp64
@@ -616,6 +634,8 @@ def run_ours(args, spec):
             line["variants"] = variants
         print(json.dumps(line), flush=True)
     g.close()
+    if de is not dp:
+        de.finalize()
     dp.finalize()
     if ws > 1:
         torch.distributed.destroy_process_group()

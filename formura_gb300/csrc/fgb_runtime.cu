@@ -915,13 +915,24 @@ int fgb_state_device(fgb_grid* g, void** ptrs, int nfields) {
 
 int64_t fgb_launch_count(fgb_grid* g) { return g ? g->launches : -1; }
 
+// A refused registration leaves the memory pageable (copies still work,
+// more slowly).  Its error is not sticky, so it is cleared here: otherwise
+// the runtime would report it again at the next launch check.
 int fgb_host_register(void* ptr, size_t bytes) {
-  FGB_CUDA(cudaHostRegister(ptr, bytes, cudaHostRegisterDefault), "host register");
+  const cudaError_t e = cudaHostRegister(ptr, bytes, cudaHostRegisterDefault);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return cuda_fail(e, "host register");
+  }
   return FGB_OK;
 }
 
 int fgb_host_unregister(void* ptr) {
-  FGB_CUDA(cudaHostUnregister(ptr), "host unregister");
+  const cudaError_t e = cudaHostUnregister(ptr);
+  if (e != cudaSuccess) {
+    (void)cudaGetLastError();
+    return cuda_fail(e, "host unregister");
+  }
   return FGB_OK;
 }
 
