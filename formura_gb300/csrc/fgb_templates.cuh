@@ -141,19 +141,18 @@ struct F64Exact {
     halves(q0, qlo, qhi);
     halves(r, rlo, rhi);
     halves(c, clo, chi);
-    const int et = (int)((chi >> 20) & 0x7ffu) + (int)((qhi >> 20) & 0x7ffu) - 1076;   // of |c| * ulp(q0) / 2
+    const unsigned eq = (qhi >> 20) & 0x7ffu, ec = (chi >> 20) & 0x7ffu;
+    const unsigned long long m = ((unsigned long long)(qhi & 0xfffffu) << 32) | qlo;
+    const int et = (int)ec + (int)eq - 1076;   // exponent field of |c| * ulp(q0) / 2
     const bool zero = is_zero(x);
-    // q0's low word away from 0, 1 and its two largest values: then q0 lies
-    // at least two ulps inside its binade, and a neighbour differs from it
-    // in the low word only
-    fits = zero || (qlo - 2u <= 0xfffffffbu && (unsigned)(et - 2) <= 2044u);
-    const unsigned thi = (chi & 0xfffffu) | ((unsigned)et << 20), ahi = rhi & 0x7fffffffu;
-    const bool gt = ahi > thi || (ahi == thi && rlo > clo);
-    const bool tie = ahi == thi && rlo == clo;
-    const bool step = gt || (tie && (qlo & 1u));
+    fits = zero || (m - 2ull <= (1ull << 52) - 5ull && (unsigned)(et - 2) <= 2044u);
+    const unsigned long long t = ((unsigned long long)((chi & 0xfffffu) | ((unsigned)et << 20)) << 32) | clo;
+    const unsigned long long a = ((unsigned long long)(rhi & 0x7fffffffu) << 32) | rlo;
+    const bool step = a > t || (a == t && (qlo & 1u));
     const bool up = ((rhi ^ chi ^ qhi) >> 31) == 0;   // towards x/c the magnitude grows
-    const unsigned lo = qlo + (step ? (up ? 1u : 0xffffffffu) : 0u);
-    return zero ? q0 : join(lo, qhi);
+    const unsigned long long qb = ((unsigned long long)qhi << 32) | qlo;
+    const unsigned long long res = qb + (step ? (up ? 1ull : ~0ull) : 0ull);
+    return zero ? q0 : join((unsigned)res, (unsigned)(res >> 32));
   }
   // RN(x / c) inside Markstein's window: two FP64 instructions and the
   // integer step where it applies to every lane of the warp, else

@@ -1,8 +1,7 @@
 /* Host check of the bit-faithful FP64 policy's quotient with its last
  * rounding step on the integer pipe (fgb::F64Exact::round_quotient):
  * y = RN(1/c), q0 = RN(x*y), r = x - q0*c (one fma, exact), and then, where
- * q0's low word is away from its extremes (so q0 lies at least two ulps
- * inside its binade), RN(x/c) is q0 or the
+ * q0 lies at least two ulps inside its binade, RN(x/c) is q0 or the
  * neighbour towards x/c: the neighbour when |r| > |c| * ulp(q0) / 2, the
  * even one of the two when |r| equals it.  The same integer steps as the
  * device code, on the host's correctly rounded fma; compared with the
@@ -33,16 +32,17 @@ static double round_quotient(double x, double c, double q0, double r, int* fits)
   const unsigned qhi = (unsigned)(qb >> 32), qlo = (unsigned)qb;
   const unsigned rhi = (unsigned)(rb >> 32), rlo = (unsigned)rb;
   const unsigned chi = (unsigned)(cb >> 32), clo = (unsigned)cb;
-  const int et = (int)((chi >> 20) & 0x7ffu) + (int)((qhi >> 20) & 0x7ffu) - 1076;
+  const unsigned eq = (qhi >> 20) & 0x7ffu, ec = (chi >> 20) & 0x7ffu;
+  const uint64_t m = ((uint64_t)(qhi & 0xfffffu) << 32) | qlo;
+  const int et = (int)ec + (int)eq - 1076;
   const int zero = ((bits(x) << 1) == 0);
-  *fits = zero || (qlo - 2u <= 0xfffffffbu && (unsigned)(et - 2) <= 2044u);
-  const unsigned thi = (chi & 0xfffffu) | ((unsigned)et << 20), ahi = rhi & 0x7fffffffu;
-  const int gt = ahi > thi || (ahi == thi && rlo > clo);
-  const int tie = ahi == thi && rlo == clo;
-  const int step = gt || (tie && (qlo & 1u));
+  *fits = zero || ((m - 2u <= (1ull << 52) - 5u) && (unsigned)(et - 2) <= 2044u);
+  const uint64_t t = ((uint64_t)((chi & 0xfffffu) | ((unsigned)et << 20)) << 32) | clo;
+  const uint64_t a = ((uint64_t)(rhi & 0x7fffffffu) << 32) | rlo;
+  const int step = a > t || (a == t && (qlo & 1u));
   const int up = ((rhi ^ chi ^ qhi) >> 31) == 0;
-  const unsigned lo = qlo + (step ? (up ? 1u : 0xffffffffu) : 0u);
-  return zero ? q0 : from(((uint64_t)qhi << 32) | lo);
+  const uint64_t res = qb + (step ? (up ? 1ull : ~0ull) : 0ull);
+  return zero ? q0 : from(res);
 }
 
 /* the device's path for numerators below the window (F64Exact::divu_outside),
