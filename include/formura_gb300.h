@@ -84,12 +84,18 @@ int64_t fgb_launch_count(fgb_grid* grid);
 
 /* Temporal-blocking kernels.  Programs whose step is a single stage also
  * have kernels that advance several steps per launch in shared-memory tiles
- * (they replace the reference's CPU temporal blocking, Templates.hs:311-381).
+ * (they replace the reference's CPU temporal blocking, Templates.hs:311-381);
+ * 3D programs also have one-step kernels on row vectors, and multi-stage 3D
+ * programs in FP32/FP16 a one-launch kernel with every stage's arrays in
+ * shared memory.
  * fgb_autotune times every variant that fits on this device and the
  * one-step kernel over `trial_steps` steps, restores the state, and selects
  * the fastest; fgb_set_variant selects one by index (-1: one step per
- * launch).  FP64 and FP32 results do not depend on the choice; with FP16
- * storage the tiles keep FP32 values between the steps of one launch. */
+ * launch).  FP64 results do not depend on the choice, nor do FP32 results
+ * of single-stage programs; the FP32 results of the one-launch multi-stage
+ * kernels agree with the stage kernels' to rounding (nvcc fuses products and
+ * sums into FMAs differently in different kernels).  With FP16 storage the
+ * tiles keep FP32 values between the steps of one launch. */
 int fgb_variant_count(fgb_grid* grid);
 int fgb_variant_info(fgb_grid* grid, int index, int* tile_x, int* tile_y, int* steps);
 int fgb_set_variant(fgb_grid* grid, int index);
