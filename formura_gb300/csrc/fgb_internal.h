@@ -110,6 +110,12 @@ struct FgbProgramDesc {
   int adj_pairs[FGB_MAX_STAGES];
   int adj_parts[FGB_MAX_STAGES];   // partial-sum kernels per stage
   int adj_recompute[FGB_MAX_STAGES];   // forward arrays of the stage read by the partial sums
+  // The forward stages whose arrays the adjoint reads, and how many arrays
+  // they store: the program's own stored arrays, which may differ from the
+  // ones the forward step stores (the generator chooses those for HBM
+  // traffic); the same as launch / nmids when they do not differ.
+  FgbStageLaunch adj_launch[FGB_NUM_PRECISIONS][FGB_MAX_STAGES];
+  int nmids_adj;
   // Uniform-table slots of the grid-independent divisors; when all of them
   // are powers of two for a grid, its FP64 steps use launch_p2, whose
   // division by them is one product.

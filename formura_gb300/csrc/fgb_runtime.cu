@@ -314,7 +314,8 @@ int fgb_open(const char* program, const int* shape, int ndim, int precision, con
   const size_t es = storage_size(precision), cs = compute_size(precision);
   cudaError_t e = cudaStreamCreateWithFlags(&g->stream, cudaStreamNonBlocking);
   for (int b = 0; b < 2 && e == cudaSuccess; ++b) e = cudaMalloc(&g->state[b], cells * d->nfields * es);
-  if (e == cudaSuccess && d->nmids > 0) e = cudaMalloc(&g->mids, cells * d->nmids * cs);
+  const int nmids = std::max(d->nmids, d->nmids_adj);   // the forward's arrays, or the adjoint's
+  if (e == cudaSuccess && nmids > 0) e = cudaMalloc(&g->mids, cells * nmids * cs);
   if (e == cudaSuccess && d->nuniforms > 0) e = cudaMalloc(&g->uniforms, d->nuniforms * cs);
   if (e == cudaSuccess && precision >= FGB_F32) e = cudaMalloc((void**)&g->staging, cells * d->nfields * 8);
   if (precision == FGB_F64 && d->ndivisors > 0) {
@@ -564,8 +565,8 @@ static int ensure_adjoint(fgb_grid* g) {
     const size_t cs = compute_size(g->precision);
     int most = 0;
     for (int s = 0; s < g->prog->nstages; ++s) most = std::max(most, g->prog->adj_pairs[s]);
-    if (!g->lam_mids && g->prog->nmids > 0)
-      FGB_CUDA(cudaMalloc(&g->lam_mids, g->cells * g->prog->nmids * cs), "adjoint of the forward arrays");
+    if (!g->lam_mids && g->prog->nmids_adj > 0)
+      FGB_CUDA(cudaMalloc(&g->lam_mids, g->cells * g->prog->nmids_adj * cs), "adjoint of the forward arrays");
     if (!g->pairs && most > 0) FGB_CUDA(cudaMalloc(&g->pairs, g->cells * most * cs), "adjoint partial sums");
   }
   return FGB_OK;
@@ -611,6 +612,9 @@ static int stage_adjoint_step(fgb_grid* g, const void* u) {
   FgbLaunch L;
   fill_launch(g, g->cur, &L);
   for (int f = 0; f < d->nfields; ++f) L.in[f] = (const char*)u + f * g->cells * es;
+  // the program's own arrays, which the adjoint reads (the buffer holds
+  // the larger of the two counts)
+  for (int k = 0; k < d->nmids_adj; ++k) L.mid[k] = (char*)g->mids + k * g->cells * cs;
   // The arrays recomputed here only feed the partial sums, which evaluate
   // their own forward values in contracted arithmetic: in the FP64 form
   // they are recomputed with the contracted FP64 kernels too (same storage,
@@ -618,7 +622,7 @@ static int stage_adjoint_step(fgb_grid* g, const void* u) {
   const int rp = g->precision == FGB_F64 ? FGB_F64_FAST : g->precision;
   for (int st = 0; st + 1 < d->nstages; ++st) {
     if (!d->adj_recompute[st]) continue;
-    cudaError_t e = d->launch[rp][st](&L, g->stream);
+    cudaError_t e = d->adj_launch[rp][st](&L, g->stream);
     if (e != cudaSuccess) return cuda_fail(e, "stage launch");
     ++g->launches;
   }
@@ -630,7 +634,7 @@ static int stage_adjoint_step(fgb_grid* g, const void* u) {
     A.lprev[f] = (char*)g->lam[g->lcur ^ 1] + f * g->cells * es;
     A.scale[f] = g->scale[f];
   }
-  for (int k = 0; k < d->nmids; ++k) {
+  for (int k = 0; k < d->nmids_adj; ++k) {
     A.mid[k] = (const char*)g->mids + k * g->cells * cs;
     A.lmid[k] = (char*)g->lam_mids + k * g->cells * cs;
   }

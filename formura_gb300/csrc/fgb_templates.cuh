@@ -903,12 +903,51 @@ struct StageAdjointFill<Prog, AdjointStages<Rec, Pairs...>> {
   }
 };
 
+// Programs whose forward step stores other arrays than the program's own
+// (see the generator's store_shared_operands) carry the program's own
+// forward stages for the adjoint: Prog::AdjProg and Prog::AdjStages.
+template <class... S>
+struct StageTypes {};
+template <class P, class = void>
+struct AdjStagesOf {
+  using type = void;
+};
+template <class P>
+struct AdjStagesOf<P, std::void_t<typename P::AdjStages>> {
+  using type = typename P::AdjStages;
+};
+template <class Prog, class List>
+struct AdjStagesFill {
+  static void fill(FgbProgramDesc&) {}
+};
+template <class Prog, class... S>
+struct AdjStagesFill<Prog, StageTypes<S...>> {
+  using AP = typename Prog::AdjProg;
+  static_assert(sizeof...(S) == Prog::kStages && AP::kStages == Prog::kStages, "the adjoint's stages are the step's");
+  static_assert(AP::kMids <= FGB_MAX_MIDS, "too many intermediate arrays");
+  template <int P>
+  static void fill_p(FgbProgramDesc& d) {
+    FgbStageLaunch l[] = {&launch_stage<AP, P, S>...};
+    for (int i = 0; i < (int)sizeof...(S); ++i) d.adj_launch[P][i] = l[i];
+  }
+  static void fill(FgbProgramDesc& d) {
+    fill_p<0>(d);
+    fill_p<1>(d);
+    fill_p<2>(d);
+    fill_p<3>(d);
+    d.nmids_adj = AP::kMids;
+  }
+};
+
 template <class Prog, class... Stages>
 struct ProgramBuilder {
   template <int P>
   static void fill(FgbProgramDesc& d) {
     FgbStageLaunch l[] = {&launch_stage<Prog, P, Stages>...};
-    for (int i = 0; i < (int)sizeof...(Stages); ++i) d.launch[P][i] = l[i];
+    for (int i = 0; i < (int)sizeof...(Stages); ++i) {
+      d.launch[P][i] = l[i];
+      d.adj_launch[P][i] = l[i];
+    }
   }
   static FgbProgramDesc make(const char* name, const char* const* fields) {
     static_assert(sizeof...(Stages) == Prog::kStages, "stage count");
@@ -920,6 +959,7 @@ struct ProgramBuilder {
     d.dim = Prog::kDim;
     d.nfields = Prog::kFields;
     d.nmids = Prog::kMids;
+    d.nmids_adj = Prog::kMids;
     d.nstages = Prog::kStages;
     d.sleeve = Prog::kSleeve;
     d.shift = Prog::kShift;
@@ -943,6 +983,7 @@ struct ProgramBuilder {
     FusedFill<Prog, Stages...>::template fill<3>(d);
     AdjointFill<typename Prog::Adjoint>::fill(d);
     StageAdjointFill<Prog, typename Prog::StageAdjoint>::fill(d);
+    AdjStagesFill<Prog, typename AdjStagesOf<Prog>::type>::fill(d);
     return d;
   }
 };

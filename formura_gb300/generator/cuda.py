@@ -35,8 +35,11 @@ from decimal import Decimal, localcontext
 from fractions import Fraction
 from typing import Dict, List, Optional, Set, Tuple
 
-from .manifest import MMNode, MMProgram, MicroNode, calc_range
-from .translate import FormuraCompileError
+import copy
+import dataclasses
+
+from .manifest import MMNode, MMProgram, MicroNode, calc_range, manifest_graph
+from .translate import FormuraCompileError, Graph
 
 
 # --------------------------------------------------------------------------
@@ -610,12 +613,18 @@ class _ProgramEmitter:
             self.table.append(entry)
         return self.table.index(entry)
 
-    def emit(self) -> KernelProgram:
+    def emit(self, ns: Optional[str] = None, define: bool = True, stage_adjoint_type: Optional[str] = None,
+             prog_extra: str = "") -> KernelProgram:
+        """The program's device code in namespace `ns` (default
+        fgb_gen_<name>), registered as a library program when `define`.
+        `stage_adjoint_type` names a stage-adjoint list emitted elsewhere and
+        `prog_extra` adds members to struct Prog."""
+        ns = ns or f"fgb_gen_{self.name}"
         out = [f"// Device code generated by formura_gb300.generator.cuda for program '{self.name}'.",
                f"// Stencil expressions come from the program's step function; the kernel",
                f"// templates live in fgb_templates.cuh.",
                '#include "fgb_templates.cuh"', "",
-               f"namespace fgb_gen_{self.name} {{", ""]
+               f"namespace {ns} {{", ""]
         stage_texts = []
         for st in self.stages:
             count = _StageEmitter(self, st)      # a pass that counts quotients per denominator
@@ -655,9 +664,11 @@ class _ProgramEmitter:
         div_count = len(div_slots) if self.divisor_slots is not None else -1
         div_list = ", ".join(str(i) for i in div_slots) if div_slots else "0"
         out.append(self.stage_reads())
+        sa = stage_adjoint_type or ('StageAdjointList' if stage_adj else 'void')
         out.append(f"struct Prog {{\n"
                    f"  using Adjoint = {'AdjointStep' if adj_src else 'void'};\n"
-                   f"  using StageAdjoint = {'StageAdjointList' if stage_adj else 'void'};\n"
+                   f"  using StageAdjoint = {sa};\n"
+                   f"{prog_extra}"
                    f"  static constexpr int kDim = {self.dim};\n"
                    f"  static constexpr int kFields = {len(self.fields)};\n"
                    f"  static constexpr int kMids = {len(self.mids)};\n"
@@ -673,11 +684,12 @@ class _ProgramEmitter:
                    f"  static constexpr int kDivisors[{max(1, len(div_slots))}] = {{{div_list}}};\n"
                    f"}};\n")
         out += stage_texts
-        out.append(f"}}  // namespace fgb_gen_{self.name}\n")
-        stage_list = ", ".join(f"fgb_gen_{self.name}::Stage{i}" for i in range(len(self.stages)))
-        names = ", ".join(f'"{f}"' for f in self.fields)
-        out.append(f"static const char* const fgb_fields_{self.name}[] = {{{names}}};")
-        out.append(f"FGB_DEFINE_PROGRAM({self.name}, fgb_gen_{self.name}::Prog, fgb_fields_{self.name}, {stage_list})")
+        out.append(f"}}  // namespace {ns}\n")
+        if define:
+            stage_list = ", ".join(f"{ns}::Stage{i}" for i in range(len(self.stages)))
+            names = ", ".join(f'"{f}"' for f in self.fields)
+            out.append(f"static const char* const fgb_fields_{self.name}[] = {{{names}}};")
+            out.append(f"FGB_DEFINE_PROGRAM({self.name}, {ns}::Prog, fgb_fields_{self.name}, {stage_list})")
         return KernelProgram(self.name, self.dim, list(self.mm.om.genv.axes), list(self.fields),
                              self.sleeve, self.shift, self.reach, self.stages,
                              self.mids, list(self.table), self.runtime_params, "\n".join(out) + "\n")
@@ -694,6 +706,80 @@ def library_option(program: str, key: str, default=None):
         return decode_config(f.read()).gpu.get(key, default)
 
 
+def store_shared_operands(g: Graph) -> Optional[Graph]:
+    """The arrays the GPU step stores, chosen for HBM traffic.  Where two or
+    more manifest nodes are each a state value plus or minus a constant times
+    one shared non-manifest value X (MUSCL reconstruction: qL = q - s/2 and
+    qR = q + s/2 from one limited slope s), X becomes the stored array and
+    those nodes are evaluated at every point that reads them, from X and the
+    state: one array instead of two or three, and one multiply-add per read.
+    The operations and their order are the program's, so the results are
+    the same bits.  None when no node fits."""
+    shared: Dict[int, List[int]] = {}
+    for i, nd in enumerate(g.nodes):
+        inst = nd.inst
+        if not nd.manifest or inst[0] != "binop" or inst[1] not in ("+", "-"):
+            continue
+        if g[inst[2]].inst[0] != "load":
+            continue
+        b = g[inst[3]]
+        if b.manifest or b.inst[0] != "binop" or b.inst[1] != "*":
+            continue
+        x, y = b.inst[2], b.inst[3]
+        xo = y if g[x].inst[0] == "imm" else (x if g[y].inst[0] == "imm" else None)
+        if xo is None or g[xo].manifest or g[xo].inst[0] in ("imm", "load", "loadindex"):
+            continue
+        if g[xo].type != nd.type:
+            continue
+        shared.setdefault(xo, []).append(i)
+    groups = {x: ns for x, ns in shared.items() if len(ns) >= 2}
+    if not groups:
+        return None
+    g2 = Graph()
+    g2.nodes = list(g.nodes)
+    for x, ns in groups.items():
+        g2.nodes[x] = dataclasses.replace(g.nodes[x], manifest=True)
+        for i in ns:
+            g2.nodes[i] = dataclasses.replace(g.nodes[i], manifest=False)
+    return g2
+
+
+def gpu_step_program(mm: MMProgram) -> MMProgram:
+    """The program as the GPU step evaluates it: the same graph, with the
+    stored arrays chosen by store_shared_operands."""
+    g2 = store_shared_operands(mm.om.step_graph)
+    if g2 is None:
+        return mm
+    om2 = dataclasses.replace(mm.om, step_graph=g2)
+    return dataclasses.replace(mm, om=om2, step=manifest_graph(g2, mm.om.genv.dimension))
+
+
+def _emit_with_own_adjoint(mm: MMProgram, mm2: MMProgram, name: str,
+                           runtime_params: List[str]) -> Optional[KernelProgram]:
+    """A program whose GPU step stores other arrays (mm2) than the program's
+    own (mm) and that has a stage adjoint: the forward steps come from mm2,
+    the adjoint and the forward stages that recompute its arrays from mm (the
+    partial sums are generated for those arrays; generated for mm2's they
+    would read the state at many more cursors).  Both share one uniform
+    table: the forward's starts with the adjoint's entries.  None when the
+    two have different stage counts."""
+    adj = _ProgramEmitter(mm, name, runtime_params, "step", True)
+    fwd = _ProgramEmitter(mm2, name, runtime_params, "step", False)
+    if len(adj.stages) != len(fwd.stages):
+        return None
+    ans = f"fgb_gen_{name}_adj"
+    adj_kp = adj.emit(ns=ans, define=False)
+    fwd.table = list(adj.table)
+    stages = ", ".join(f"{ans}::Stage{i}" for i in range(len(adj.stages)))
+    extra = (f"  // the program's own forward stages, whose arrays the adjoint reads\n"
+             f"  using AdjProg = {ans}::Prog;\n"
+             f"  using AdjStages = fgb::StageTypes<{stages}>;\n")
+    kp = fwd.emit(stage_adjoint_type=f"{ans}::StageAdjointList", prog_extra=extra)
+    kp.source = adj_kp.source + "\n" + kp.source
+    kp.graph = "step"
+    return kp
+
+
 def emit_cuda(mm: MMProgram, name: str, runtime_params: Optional[List[str]] = None,
               graph: str = "step", stage_adjoint: Optional[bool] = None) -> KernelProgram:
     """Device code of the step function (or of first_step / filter, which
@@ -702,6 +788,14 @@ def emit_cuda(mm: MMProgram, name: str, runtime_params: Optional[List[str]] = No
     when the library's program sets `gpu_adjoint: 1`."""
     if stage_adjoint is None:
         stage_adjoint = bool(library_option(name, "gpu_adjoint", 0))
+    if graph == "step":
+        mm2 = gpu_step_program(mm)
+        if mm2 is not mm and stage_adjoint:
+            kp = _emit_with_own_adjoint(mm, mm2, name, runtime_params or [])
+            if kp is not None:
+                return kp
+        else:
+            mm = mm2
     kp = _ProgramEmitter(mm, name if graph == "step" else f"{name}__{graph}",
                          runtime_params or [], graph, stage_adjoint and graph == "step").emit()
     kp.graph = graph

@@ -31,6 +31,9 @@ struct AdjointStagePair {
 };
 template <class... Parts>
 struct AdjParts {};
+// the program's own forward stages, when the forward step stores other arrays
+template <class... S>
+struct StageTypes {};
 }  // namespace fgb
 
 namespace hostshim {
@@ -178,15 +181,43 @@ void sweep(Grid& g) {
       }
 }
 
+// The forward stages the adjoint recomputes its arrays with, and how many
+// arrays they store: Prog::AdjStages / Prog::AdjProg where the program has
+// them, else the step's own.
+template <class Prog, class = void>
+struct AdjForward {
+  template <class Own>
+  static Own stages(Own o) { return o; }
+  static constexpr int kMids = Prog::kMids;
+};
+template <class Prog>
+struct AdjForward<Prog, std::void_t<typename Prog::AdjStages>> {
+  template <class Own>
+  static typename Prog::AdjStages stages(Own) { return {}; }
+  static constexpr int kMids = Prog::AdjProg::kMids;
+};
+
+template <class Acc, class Rec, class List>
+struct Recompute;
+template <class Acc, class Rec, class... S>
+struct Recompute<Acc, Rec, fgb::StageTypes<S...>> {
+  static void run(Grid& g) {
+    int s = 0;
+    ((Rec::kStage[s++] ? sweep<Acc, S>(g) : void()), ...);
+  }
+};
+
 template <class Prog, class... Stages>
 struct Runner {
   using FwdAcc = Fwd<Prog::kDim, Prog::kShift>;
+  using AF = AdjForward<Prog>;
   static void init(Grid& g, const int* n, const double* U) {
     for (int a = 0; a < 3; ++a) g.n[a] = 1;
     for (int a = 0; a < Prog::kDim; ++a) g.n[3 - Prog::kDim + a] = n[a];
     g.cells = (size_t)g.n[0] * g.n[1] * g.n[2];
     g.U = U;
-    g.mids.assign((size_t)Prog::kMids * g.cells + 1, 0.0);
+    const int nm = Prog::kMids > AF::kMids ? Prog::kMids : AF::kMids;
+    g.mids.assign((size_t)nm * g.cells + 1, 0.0);
   }
   static void forward(Grid& g, int upto) {   // stages [0, upto)
     int s = 0;
@@ -207,14 +238,9 @@ struct Runner {
     }
     (void)most;
   }
-  template <class Rec, class... Pairs>
-  static void recompute_flags(Grid& g, fgb::AdjointStages<Rec, Pairs...>) {
-    recompute<Rec>(g);
-  }
-  template <class Rec>
-  static void recompute(Grid& g) {
-    int s = 0;
-    ((Rec::kStage[s++] ? sweep<FwdAcc, Stages>(g) : void()), ...);
+  template <class Rec, class... Pairs, class List>
+  static void recompute_flags(Grid& g, fgb::AdjointStages<Rec, Pairs...>, List) {
+    Recompute<FwdAcc, Rec, List>::run(g);
   }
   template <class Rec, class... Pairs, size_t... I>
   static void reverse_pairs(Grid& g, fgb::AdjointStages<Rec, Pairs...>, std::index_sequence<I...>) {
@@ -228,8 +254,8 @@ struct Runner {
       sweep<Adj1, typename Prog::Adjoint>(g);
       return 0;
     } else if constexpr (!std::is_same<typename Prog::StageAdjoint, void>::value) {
-      recompute_flags(g, typename Prog::StageAdjoint{});
-      g.lmids.assign((size_t)Prog::kMids * g.cells + 1, 0.0);
+      recompute_flags(g, typename Prog::StageAdjoint{}, AF::stages(fgb::StageTypes<Stages...>{}));
+      g.lmids.assign((size_t)AF::kMids * g.cells + 1, 0.0);
       reverse_pairs(g, typename Prog::StageAdjoint{}, std::make_index_sequence<Prog::kStages>{});
       return 0;
     } else {
