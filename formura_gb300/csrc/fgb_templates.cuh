@@ -254,6 +254,35 @@ struct F64Exact {
     return __ddiv_rn(a, b);
   }
   static __device__ __forceinline__ T neg(T a) { return -a; }
+  // RN(1 - x) for the literal 1 (Gray-Scott's feed term F*(1 - u)).  For x
+  // in [0.5, 2) the difference is exact (Sterbenz's lemma): with
+  // x = X * 2^-53, X an integer below 2^54, 1 - x = (2^53 - X) * 2^-53, and
+  // that integer is normalised by its leading bit on the integer pipe; 1 - 1
+  // is +0 as in round-to-nearest.  A warp with a lane outside the range
+  // subtracts on the FP64 pipe (the same bits).
+  static __device__ __forceinline__ bool one_minus_window(T x) {
+    unsigned lo, hi;
+    halves(x, lo, hi);
+    return (hi >> 21) == 511u;   // sign 0, exponent field 1022 or 1023
+  }
+  static __device__ __forceinline__ T one_minus_exact(T x) {
+    unsigned lo, hi;
+    halves(x, lo, hi);
+    const unsigned long long X = ((((unsigned long long)((hi & 0xfffffu) | 0x100000u)) << 32) | lo) << ((hi >> 20) & 1u);
+    const long long d = (long long)(1ull << 53) - (long long)X;
+    const unsigned long long a = d < 0 ? (unsigned long long)(-d) : (unsigned long long)d;
+    const int n = __clzll((long long)a);   // 10 <= n <= 64
+    // leading bit to position 52; it carries into the exponent field
+    const unsigned long long b = ((unsigned long long)(1032 - n) << 52) + (a << ((n - 11) & 63));
+    const unsigned long long r = a == 0ull ? 0ull : (b | (d < 0 ? 0x8000000000000000ull : 0ull));
+    return join((unsigned)r, (unsigned)(r >> 32));
+  }
+  static __device__ __forceinline__ T one_minus(T x) {
+    if (warp_all(one_minus_window(x))) return one_minus_exact(x);
+    return one_minus_ieee(x);
+  }
+  // out of line, so that the compiler does not compute it ahead of the test
+  static __device__ __noinline__ T one_minus_ieee(T x) { return __dsub_rn(1.0, x); }
   static __device__ __forceinline__ T sqrt(T a) { return __dsqrt_rn(a); }
   // |a| by clearing the sign bit on the integer pipe (exact, NaN included)
   static __device__ __forceinline__ T fabs(T a) {
@@ -291,6 +320,7 @@ struct F64Ieee {
   static __device__ __forceinline__ T rcp(T b) { return __drcp_rn(b); }
   static __device__ __forceinline__ T divr(T a, T b, T, bool&) { return __ddiv_rn(a, b); }
   static __device__ __forceinline__ T neg(T a) { return -a; }
+  static __device__ __forceinline__ T one_minus(T x) { return __dsub_rn(1.0, x); }
   static __device__ __forceinline__ T sqrt(T a) { return __dsqrt_rn(a); }
   static __device__ __forceinline__ T fabs(T a) { return ::fabs(a); }
   static __device__ __forceinline__ T exp(T a) { return ::exp(a); }
@@ -332,6 +362,7 @@ struct F64Fast {
   static __device__ __forceinline__ T rcp(T b) { return __drcp_rn(b); }
   static __device__ __forceinline__ T divr(T a, T, T y, bool&) { return a * y; }
   static __device__ __forceinline__ T neg(T a) { return -a; }
+  static __device__ __forceinline__ T one_minus(T x) { return 1.0 - x; }
   static __device__ __forceinline__ T sqrt(T a) { return ::sqrt(a); }
   static __device__ __forceinline__ T fabs(T a) { return ::fabs(a); }
   static __device__ __forceinline__ T exp(T a) { return ::exp(a); }
@@ -369,6 +400,7 @@ struct F32 {
   static __device__ __forceinline__ T rcp(T b) { return __fdividef(1.0f, b); }
   static __device__ __forceinline__ T divr(T a, T, T y, bool&) { return a * y; }
   static __device__ __forceinline__ T neg(T a) { return -a; }
+  static __device__ __forceinline__ T one_minus(T x) { return 1.0f - x; }
   static __device__ __forceinline__ T sqrt(T a) { return sqrtf(a); }
   static __device__ __forceinline__ T fabs(T a) { return fabsf(a); }
   static __device__ __forceinline__ T exp(T a) { return expf(a); }

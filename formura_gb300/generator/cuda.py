@@ -456,6 +456,8 @@ class _StageEmitter:
                 if a[0] == "scaled":
                     rhs = self.as_T(b) if op == "+" else f"{self.P}::neg({self.as_T(b)})"
                     return self.bind(f"{self.P}::fma(T({c_double(a[1])}), {self.as_T(a[2])}, {rhs}, fgb_ok)")
+                if op == "-" and a[0] == "lit" and a[1] == 1.0:
+                    return self.bind(f"{self.P}::one_minus({self.as_T(b)})")
                 fn = "add" if op == "+" else "sub"
                 return self.bind(f"{self.P}::{fn}({self.as_T(a)}, {self.as_T(b)})")
             if op == "/":

@@ -1,5 +1,6 @@
 // GPU check of the shortened operations of the bit-faithful FP64 policy
-// (fgb::F64Exact::divu, ::divr with ::rcp, ::fma with a power-of-two factor)
+// (fgb::F64Exact::divu, ::divr with ::rcp, ::fma with a power-of-two factor,
+// ::one_minus)
 // against the reference's separately rounded IEEE operations, bit for bit,
 // wherever the form's range flag stays set.  Operand classes: moderate, wide,
 // subnormal and tiny, huge and non-finite, signed zeros, any bit pattern.
@@ -47,9 +48,12 @@ __device__ __forceinline__ bool same(double a, double b) {
 // stays set (where it drops, the kernels evaluate with F64Ieee instead).
 // Counts per operation: mismatches, and lanes inside the shortened window;
 // then the mismatches of the integer-pipe comparisons, and of the divisions'
-// integer rounding step taken lane by lane, with the lanes it applied to.
+// integer rounding step taken lane by lane, with the lanes it applied to;
+// then the mismatches of 1 - x (warp by warp, and its integer form lane by
+// lane) with the lanes in that form's window.
 __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
   unsigned long long bad[4] = {0, 0, 0, 0}, fast[3] = {0, 0, 0}, step_used = 0, step_bad = 0;
+  unsigned long long om_bad = 0, om_used = 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
     const uint64_t key = seed * 0x100000000ull + i;
@@ -108,6 +112,18 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
                         F64Exact::ge(p, q), F64Exact::eq(p, q), F64Exact::ne(p, q)};
     for (int j = 0; j < 6; ++j) bad[3] += hw[j] != in[j];
     bad[3] += !same(F64Exact::fabs(p), fabs(p)) || (__double_as_longlong(F64Exact::fabs(p)) >> 63) != 0;
+    // 1 - x: whole warps in [0.5, 2), warps with one lane outside, and any
+    // operand class
+    const int cm = (int)(mix(warp * 13 + seed) % 3);
+    const uint64_t sm = mix(key ^ 3);
+    double u = __longlong_as_double((long long)(((1022ull + (sm & 1)) << 52) | ((sm >> 1) & 0x000fffffffffffffull)));
+    if (cm == 1 && (i & 31) == (warp & 31)) u = operand(key * 7 + 7, (int)(sm % 6));
+    if (cm == 2) u = operand(key * 7 + 7, (int)(sm % 6));
+    om_bad += !same(F64Exact::one_minus(u), __dsub_rn(1.0, u));
+    if (F64Exact::one_minus_window(u)) {
+      ++om_used;
+      om_bad += !same(F64Exact::one_minus_exact(u), __dsub_rn(1.0, u));
+    }
   }
   for (int j = 0; j < 3; ++j) {
     atomicAdd(&out[j], bad[j]);
@@ -116,15 +132,17 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
   atomicAdd(&out[6], bad[3]);
   atomicAdd(&out[7], step_bad);
   atomicAdd(&out[8], step_used);
+  atomicAdd(&out[9], om_bad);
+  atomicAdd(&out[10], om_used);
 }
 
 extern "C" int exact_forms_gpu_check(unsigned long long seed, unsigned long long n, unsigned long long* host_out) {
   unsigned long long* d = nullptr;
-  if (cudaMalloc(&d, 9 * sizeof(unsigned long long)) != cudaSuccess) return 1;
-  cudaMemset(d, 0, 9 * sizeof(unsigned long long));
+  if (cudaMalloc(&d, 11 * sizeof(unsigned long long)) != cudaSuccess) return 1;
+  cudaMemset(d, 0, 11 * sizeof(unsigned long long));
   check<<<152 * 8, 256>>>(seed, n, d);
   cudaError_t e = cudaDeviceSynchronize();
-  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 9 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 11 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
   cudaFree(d);
   return e == cudaSuccess ? 0 : 2;
 }

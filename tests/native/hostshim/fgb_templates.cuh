@@ -59,6 +59,7 @@ struct Exact {
   static bool ne(T a, T b) { return a != b; }
   static T divr(T a, T b, T, bool&) { return a / b; }
   static T neg(T a) { return -a; }
+  static T one_minus(T x) { return 1.0 - x; }
   static T sqrt(T a) { return std::sqrt(a); }
   static T fabs(T a) { return std::fabs(a); }
   static T exp(T a) { return std::exp(a); }

@@ -36,3 +36,16 @@ def test_quotient_integer_rounding_step(tmp_path):
     # it applies to most cases; quotients at powers of two and exact
     # quotients with a short significand (a zero low word) take the FMA
     assert applied > 3 * skipped > 0
+
+
+def test_one_minus_integer_pipe(tmp_path):
+    """1 - x for x in [0.5, 2) on the integer pipe (exact by Sterbenz's
+    lemma), with the device's integer steps on the host: identical to the
+    IEEE subtraction on 1.2 * 10^7 values of the window, its ends and their
+    neighbours; the window test refuses exactly the values outside it."""
+    exe = str(tmp_path / "one_minus_host")
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", os.path.join(HERE, "native", "one_minus_host.c"),
+                           "-o", exe])
+    bad, cases, outside = map(int, subprocess.check_output([exe, "3000000"], text=True).split())
+    assert bad == 0
+    assert cases > 10**7 and outside > 10**6
