@@ -561,9 +561,10 @@ __device__ __forceinline__ void eval(const A& a, const typename M::U* __restrict
 // covers the contiguous (last) axis.  With RPT > 1 a thread has the loads of
 // several points in flight at once, which is what a memory-bound FP32/FP16
 // step needs to cover the HBM latency.
-// (Capping the large FP64 stages' registers for more resident blocks was
-// measured and lost: HLLD FP64 0.212 GLUP/s uncapped, 0.203 at 128
-// registers, 0.193 at 102.)
+// (Capping the FP64 stages' registers for more resident blocks was measured
+// and lost: HLLD FP64 0.212 GLUP/s uncapped, 0.203 at 128 registers, 0.193
+// at 102; Gray-Scott FP64 16.64 at 38 registers (12 blocks per SM), 16.60 at
+// 32 (16 blocks, 12 bytes spilled).)
 template <class M, class S, int DIM, int SHIFT, class Stage, int RPT>
 __global__ void __launch_bounds__(kBlockX) stage_kernel(const __grid_constant__ FgbLaunch L) {
   const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
