@@ -828,12 +828,27 @@ struct AdjDirectAccess<M, S, T, DIM, SHIFT, AdjParts<Parts...>> : AdjGatherAcces
   }
 };
 
-template <class M, class Acc, class F>
+// One thread per point of RPT consecutive rows, as in stage_kernel.
+template <class M, class Acc, class F, int RPT>
 __global__ void __launch_bounds__(kBlockX) adj_stage_kernel(const __grid_constant__ FgbAdjLaunch L) {
   const int p2 = blockIdx.x * blockDim.x + threadIdx.x;
   if (p2 >= L.n[2]) return;
-  Acc a{L, (int)blockIdx.z, (int)blockIdx.y, p2};
-  eval<M, F>(a, static_cast<const typename M::U*>(L.uniforms));
+#pragma unroll
+  for (int r = 0; r < RPT; ++r) {
+    const int p1 = (int)blockIdx.y * RPT + r;
+    if (RPT > 1 && p1 >= L.n[1]) break;
+    Acc a{L, (int)blockIdx.z, p1, p2};
+    eval<M, F>(a, static_cast<const typename M::U*>(L.uniforms));
+  }
+}
+
+template <class M, class Acc, class F, int P>
+cudaError_t launch_adj_rows(const FgbAdjLaunch* L, cudaStream_t stream) {
+  constexpr int R = rows_per_thread<P, false>();
+  const int bx = L->n[2] >= kBlockX ? kBlockX : ((L->n[2] + 31) / 32) * 32;
+  dim3 grid((L->n[2] + bx - 1) / bx, (L->n[1] + R - 1) / R, L->n[0]);
+  adj_stage_kernel<M, Acc, F, R><<<grid, bx, 0, stream>>>(*L);
+  return cudaGetLastError();
 }
 
 template <class Prog, int P, class F, bool Gather>
@@ -843,10 +858,7 @@ cudaError_t launch_adj_stage(const FgbAdjLaunch* L, cudaStream_t stream) {
   using T = typename M::T;
   using Acc = typename std::conditional<Gather, AdjGatherAccess<S, T>,
                                         AdjPartialAccess<S, T, Prog::kDim, Prog::kShift>>::type;
-  const int bx = L->n[2] >= kBlockX ? kBlockX : ((L->n[2] + 31) / 32) * 32;
-  dim3 grid((L->n[2] + bx - 1) / bx, L->n[1], L->n[0]);
-  adj_stage_kernel<M, Acc, F><<<grid, bx, 0, stream>>>(*L);
-  return cudaGetLastError();
+  return launch_adj_rows<M, Acc, F, P>(L, stream);
 }
 
 template <class Prog, int P, class Parts, class F>
@@ -854,11 +866,7 @@ cudaError_t launch_adj_direct(const FgbAdjLaunch* L, cudaStream_t stream) {
   using M = typename Precision<P>::M;
   using S = typename Precision<P>::S;
   using T = typename M::T;
-  using Acc = AdjDirectAccess<M, S, T, Prog::kDim, Prog::kShift, Parts>;
-  const int bx = L->n[2] >= kBlockX ? kBlockX : ((L->n[2] + 31) / 32) * 32;
-  dim3 grid((L->n[2] + bx - 1) / bx, L->n[1], L->n[0]);
-  adj_stage_kernel<M, Acc, F><<<grid, bx, 0, stream>>>(*L);
-  return cudaGetLastError();
+  return launch_adj_rows<M, AdjDirectAccess<M, S, T, Prog::kDim, Prog::kShift, Parts>, F, P>(L, stream);
 }
 
 template <class Partial, class Gather>
