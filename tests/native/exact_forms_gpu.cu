@@ -50,10 +50,11 @@ __device__ __forceinline__ bool same(double a, double b) {
 // then the mismatches of the integer-pipe comparisons, and of the divisions'
 // integer rounding step taken lane by lane, with the lanes it applied to;
 // then the mismatches of 1 - x (warp by warp, and its integer form lane by
-// lane) with the lanes in that form's window.
+// lane) with the lanes in that form's window; then the mismatches of the
+// quotients below 2^-1023 on the integer grid, lane by lane, with their lanes.
 __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
   unsigned long long bad[4] = {0, 0, 0, 0}, fast[3] = {0, 0, 0}, step_used = 0, step_bad = 0;
-  unsigned long long om_bad = 0, om_used = 0;
+  unsigned long long om_bad = 0, om_used = 0, sub_bad = 0, sub_used = 0;
   const uint64_t stride = (uint64_t)gridDim.x * blockDim.x;
   for (uint64_t i = blockIdx.x * (uint64_t)blockDim.x + threadIdx.x; i < n; i += stride) {
     const uint64_t key = seed * 0x100000000ull + i;
@@ -63,8 +64,18 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
     double c = operand(warp * 11 + seed, ca == 3 ? 1 : ca % 2);
     if ((warp & 3) == 3)   // powers of two, whose quotient is one product
       c = __longlong_as_double((long long)(__double_as_longlong(c) & 0xfff0000000000000ull));
+    double x = operand(key * 7 + 1, cb == 5 ? (int)(mix(key) % 6) : cb);
+    if ((warp & 7) == 6) {
+      // one warp with quotients below 2^-1023, numerators in the window and
+      // tiny numerators with a normal quotient (c in [2^10, 2^60])
+      const uint64_t rw = mix(warp * 17 + seed), r2 = mix(key * 5 + 9);
+      const int ecb = 1023 + 10 + (int)(rw % 51);
+      c = make(rw >> 63, ecb, mix(rw));
+      if (i % 3 == 0) x = make(r2 >> 63, 0, mix(r2) >> (r2 % 52));
+      else if (i % 3 == 1) x = make(r2 >> 63, 1023 - 60 + (int)(r2 % 121), mix(r2));
+      else x = make(r2 >> 63, ecb - 1021 + (int)(r2 % (uint64_t)(63 - (ecb - 1021))), mix(r2));
+    }
     const double rc = 1.0 / c;
-    const double x = operand(key * 7 + 1, cb == 5 ? (int)(mix(key) % 6) : cb);
     bool ok = true;
     if ((warp & 3) == 3) {   // the power-of-two policy's single product, for every numerator
       if (!same(fgb::F64ExactP2::divu(x, c, rc, ok), __ddiv_rn(x, c))) ++bad[0];
@@ -80,6 +91,11 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
       const double q = F64Exact::round_quotient(x, c, q0, rem, fits);
       step_used += fits;
       step_bad += fits && !same(q, __ddiv_rn(x, c));
+    }
+    // quotients below 2^-1023 on the integer grid, lane by lane
+    if (F64Exact::divu_sub(x, c)) {
+      ++sub_used;
+      sub_bad += !same(F64Exact::divu_mixed(x, c, rc, false, true), __ddiv_rn(x, c));
     }
     // divr: grid numerator and denominator
     const double a = operand(key * 7 + 2, ca == 5 ? (int)(mix(key ^ 1) % 6) : ca);
@@ -134,15 +150,17 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
   atomicAdd(&out[8], step_used);
   atomicAdd(&out[9], om_bad);
   atomicAdd(&out[10], om_used);
+  atomicAdd(&out[11], sub_bad);
+  atomicAdd(&out[12], sub_used);
 }
 
 extern "C" int exact_forms_gpu_check(unsigned long long seed, unsigned long long n, unsigned long long* host_out) {
   unsigned long long* d = nullptr;
-  if (cudaMalloc(&d, 11 * sizeof(unsigned long long)) != cudaSuccess) return 1;
-  cudaMemset(d, 0, 11 * sizeof(unsigned long long));
+  if (cudaMalloc(&d, 13 * sizeof(unsigned long long)) != cudaSuccess) return 1;
+  cudaMemset(d, 0, 13 * sizeof(unsigned long long));
   check<<<152 * 8, 256>>>(seed, n, d);
   cudaError_t e = cudaDeviceSynchronize();
-  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 11 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
+  if (e == cudaSuccess) e = cudaMemcpy(host_out, d, 13 * sizeof(unsigned long long), cudaMemcpyDeviceToHost);
   cudaFree(d);
   return e == cudaSuccess ? 0 : 2;
 }

@@ -49,3 +49,17 @@ def test_one_minus_integer_pipe(tmp_path):
     bad, cases, outside = map(int, subprocess.check_output([exe, "3000000"], text=True).split())
     assert bad == 0
     assert cases > 10**7 and outside > 10**6
+
+
+def test_subnormal_quotient_integer_grid(tmp_path):
+    """Quotients below 2^-1023 by a grid-independent constant, rounded on the
+    integer grid of the subnormals (N = RN(X/c) for X = |x| * 2^1074, from
+    RN(X * RN(1/c)) rounded to an integer and the exact remainder), with the
+    device's steps on the host: identical to RN(x/c) on about 9 * 10^6
+    cases, exact ties and exact quotients included."""
+    exe = str(tmp_path / "subnormal_quotient_host")
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off",
+                           os.path.join(HERE, "native", "subnormal_quotient_host.c"), "-o", exe, "-lm"])
+    bad, cases = map(int, subprocess.check_output([exe, "2000000"], text=True).split())
+    assert bad == 0
+    assert cases > 5 * 10**6
