@@ -196,10 +196,10 @@ struct F64Exact {
   // quotient comes back by 2^-256 exactly, both on the integer pipe, so such
   // a quotient costs what one inside the window costs.  That holds when x's
   // exponent (a subnormal's counted from its leading bit) is at least c's
-  // minus 1021.  Quotients below 2^-1023 are rounded on the integer grid of
+  // minus 1021.  Quotients below 2^-1021 are rounded on the integer grid of
   // the subnormals (divu_sub, divu_mixed below), with the same two FP64
-  // instructions; a warp with any lane in neither form (a quotient in
-  // [2^-1023, 2^-1021), or an operand out of range) takes the IEEE division.
+  // instructions; a warp with a lane in none of the forms (an operand out of
+  // range) takes the IEEE division.
   // Out of line, so that the compiler cannot fold this path into the common
   // one.
   //
@@ -236,24 +236,30 @@ struct F64Exact {
     const int eff = ex != 0u ? (int)ex : 12 - __clzll((long long)m);   // a subnormal's leading bit
     return within(c, 100) && ex < 63u && m + ex != 0ull && eff + 1021 >= (int)expo(c);
   }
-  // Quotients below 2^-1023 (subnormal ones): RN(x/c) is N * 2^-1074 for
-  // the integer N nearest X/c, ties to even, with X = |x| * 2^1074 an
-  // integer (exact on the integer pipe).  q0 = RN(X * |RN(1/c)|) lies within
-  // 0.5 + 2^-52 of X/c (below 2^51), so n0, q0 rounded to an integer, lies
-  // within 1 + 2^-52 of it; the remainder X - n0 * |c| is then exact (one
-  // FMA), and its size against |c|/2 picks N among n0 - 1, n0, n0 + 1.  The
-  // bit pattern of N * 2^-1074 is N.  Applies to a nonzero x whose exponent
-  // (a subnormal's counted from its leading bit) is at most c's minus 1024.
+  // Quotients below 2^-1021 (subnormal ones and the lowest normal binade):
+  // RN(x/c) is N * 2^-1074 for the integer N nearest X/c, ties to even, with
+  // X = |x| * 2^1074 an integer (exact on the integer pipe), since the
+  // doubles below 2^-1021 lie on that grid; the bit pattern of N * 2^-1074
+  // is N.  With q0 = RN(X * |RN(1/c)|):
+  // - below 2^51, q0 lies within 0.5 + 2^-52 of X/c, so n0, q0 rounded to an
+  //   integer, lies within 1 + 2^-52 of it; the remainder X - n0 * |c| is
+  //   then exact (one FMA), and its size against |c|/2 picks N among
+  //   n0 - 1, n0, n0 + 1;
+  // - from 2^51 (ulp 1/2 or 1), q0 lies within one ulp of X/c, so
+  //   X - q0 * |c| is exact; with q0's own fraction (0 or 1/2) it decides N
+  //   in the same way.
+  // Applies to a nonzero x whose exponent (a subnormal's counted from its
+  // leading bit) is at most c's minus 1022.
   static __device__ __forceinline__ bool divu_sub(T x, T c) {
     unsigned lo, hi;
     halves(x, lo, hi);
     const unsigned ex = (hi >> 20) & 0x7ffu;
     const unsigned long long m = ((unsigned long long)(hi & 0xfffffu) << 32) | lo;
     const int eff = ex != 0u ? (int)ex : 12 - __clzll((long long)m);
-    return within(c, 100) && m + ex != 0ull && eff - (int)expo(c) <= -1024;
+    return within(c, 100) && m + ex != 0ull && eff - (int)expo(c) <= -1022;
   }
   // A warp whose lanes each lie in the window, among the tiny numerators or
-  // among the quotients below 2^-1023: the same two FP64 instructions on
+  // among the quotients below 2^-1021: the same two FP64 instructions on
   // every lane's own operands, then the lane's integer steps.
   static __device__ __forceinline__ T divu_mixed(T x, T c, T rc, bool tiny, bool sub) {
     unsigned xl, xh, cl, ch, yl, yh;
@@ -263,8 +269,8 @@ struct F64Exact {
     const T a = sub ? scale_up<1074>(join(xl, xh & 0x7fffffffu)) : (tiny ? scale_up<256>(x) : x);
     const T cc = sub ? join(cl, ch & 0x7fffffffu) : c;
     const T q0 = __dmul_rn(a, sub ? join(yl, yh & 0x7fffffffu) : rc);
-    // q0 rounded to an integer (half up; q0 < 2^51 + 1 on the lanes below
-    // 2^-1023), and that integer as a double
+    // below 2^51: q0 rounded to an integer (half up), and that integer as a
+    // double; from 2^51: q0's integer part and whether q0 ends in a half
     unsigned ql, qh;
     halves(q0, ql, qh);
     const int e = (int)((qh >> 20) & 0x7ffu) - 1023;
@@ -274,20 +280,26 @@ struct F64Exact {
     const int lead = 63 - __clzll((long long)(n0 | 1ull));
     const unsigned long long nb =
         n0 == 0ull ? 0ull : (((unsigned long long)(lead + 1023) << 52) | ((n0 << (52 - lead)) & 0x000fffffffffffffull));
-    const T r = __fma_rn(-(sub ? join((unsigned)nb, (unsigned)(nb >> 32)) : q0), cc, a);
+    const bool upper = e >= 51;
+    const unsigned long long base = upper ? (e >= 52 ? qm << min(e - 52, 11) : qm >> 1) : n0;
+    const bool halfq = e == 51 && (qm & 1ull);
+    const T r = __fma_rn(-((sub && !upper) ? join((unsigned)nb, (unsigned)(nb >> 32)) : q0), cc, a);
     // window and tiny lanes: the integer rounding step (or Markstein's FMA)
     bool fits;
     T q = round_quotient(a, c, q0, r, fits);
     if (!warp_all(fits || sub)) {
       if (!sub) q = markstein_last(a, q0, r, rc);
     }
-    // lanes below 2^-1023: the remainder against |c|/2
+    // lanes below 2^-1021: the remainder against |c|/2, or its sign where
+    // q0 ends in a half
     unsigned rl, rh;
     halves(r, rl, rh);
     const unsigned long long ar = ((unsigned long long)(rh & 0x7fffffffu) << 32) | rl;
     const unsigned long long half = (((unsigned long long)(ch & 0x7fffffffu) << 32) | cl) - (1ull << 52);
-    const bool step = ar > half || (ar == half && (n0 & 1ull));
-    const unsigned long long n = n0 + (step ? ((rh >> 31) ? ~0ull : 1ull) : 0ull);
+    const bool rneg = (rh >> 31) != 0u;
+    const bool step = halfq ? ((!rneg && ar != 0ull) || (ar == 0ull && (base & 1ull)))
+                            : (ar > half || (ar == half && (base & 1ull)));
+    const unsigned long long n = base + (step ? ((rneg && !halfq) ? ~0ull : 1ull) : 0ull);
     const unsigned long long sb = n | ((unsigned long long)((xh ^ ch) & 0x80000000u) << 32);
     return sub ? join((unsigned)sb, (unsigned)(sb >> 32)) : (tiny ? scale_down(q) : q);
   }

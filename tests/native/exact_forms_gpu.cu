@@ -51,7 +51,7 @@ __device__ __forceinline__ bool same(double a, double b) {
 // integer rounding step taken lane by lane, with the lanes it applied to;
 // then the mismatches of 1 - x (warp by warp, and its integer form lane by
 // lane) with the lanes in that form's window; then the mismatches of the
-// quotients below 2^-1023 on the integer grid, lane by lane, with their lanes.
+// quotients below 2^-1021 on the integer grid, lane by lane, with their lanes.
 __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
   unsigned long long bad[4] = {0, 0, 0, 0}, fast[3] = {0, 0, 0}, step_used = 0, step_bad = 0;
   unsigned long long om_bad = 0, om_used = 0, sub_bad = 0, sub_used = 0;
@@ -66,12 +66,13 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
       c = __longlong_as_double((long long)(__double_as_longlong(c) & 0xfff0000000000000ull));
     double x = operand(key * 7 + 1, cb == 5 ? (int)(mix(key) % 6) : cb);
     if ((warp & 7) == 6) {
-      // one warp with quotients below 2^-1023, numerators in the window and
+      // one warp with quotients below 2^-1021, numerators in the window and
       // tiny numerators with a normal quotient (c in [2^10, 2^60])
       const uint64_t rw = mix(warp * 17 + seed), r2 = mix(key * 5 + 9);
       const int ecb = 1023 + 10 + (int)(rw % 51);
       c = make(rw >> 63, ecb, mix(rw));
-      if (i % 3 == 0) x = make(r2 >> 63, 0, mix(r2) >> (r2 % 52));
+      if (i % 3 == 0)   // quotients below 2^-1021: subnormal numerators, and the top of the range
+        x = (r2 & 2) ? make(r2 >> 63, 0, mix(r2) >> (r2 % 52)) : make(r2 >> 63, ecb - 1022 - (int)(r2 % 3), mix(r2));
       else if (i % 3 == 1) x = make(r2 >> 63, 1023 - 60 + (int)(r2 % 121), mix(r2));
       else x = make(r2 >> 63, ecb - 1021 + (int)(r2 % (uint64_t)(63 - (ecb - 1021))), mix(r2));
     }
@@ -92,7 +93,7 @@ __global__ void check(uint64_t seed, uint64_t n, unsigned long long* out) {
       step_used += fits;
       step_bad += fits && !same(q, __ddiv_rn(x, c));
     }
-    // quotients below 2^-1023 on the integer grid, lane by lane
+    // quotients below 2^-1021 on the integer grid, lane by lane
     if (F64Exact::divu_sub(x, c)) {
       ++sub_used;
       sub_bad += !same(F64Exact::divu_mixed(x, c, rc, false, true), __ddiv_rn(x, c));

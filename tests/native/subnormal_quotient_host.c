@@ -1,14 +1,18 @@
-/* Host check of the bit-faithful FP64 policy's quotient below 2^-1023
- * (fgb::F64Exact::sub_quotient): RN(x/c) is N * 2^-1074 for the integer N
- * nearest X/c (ties to even), X = |x| * 2^1074.  q0 = RN(X * |RN(1/c)|)
- * rounded to an integer gives N0 within 1 + 2^-52 of X/c; the remainder
- * X - N0*|c| is exact (one fma) and picks N among N0 - 1, N0, N0 + 1.  The
- * same integer steps as the device code, compared with the host's IEEE
- * division.  Cases: random subnormal and tiny normal numerators against
- * constants in [2^-100, 2^100] wherever the path applies, numerators at the
- * edge of its range, exact quotients, and exact ties (X/c = k + 1/2 with
- * c = 3 * 2^j).
- * Prints "mismatches cases". */
+/* Host check of the bit-faithful FP64 policy's quotient below 2^-1021
+ * (fgb::F64Exact::divu_mixed on its integer-grid lanes): RN(x/c) is
+ * N * 2^-1074 for the integer N nearest X/c (ties to even),
+ * X = |x| * 2^1074, since the doubles below 2^-1021 lie on that grid.
+ * q0 = RN(X * |RN(1/c)|).  Below 2^51, q0 rounded to an integer gives n0
+ * within 1 + 2^-52 of X/c, the remainder X - n0*|c| is exact (one fma) and
+ * picks N among n0 - 1, n0, n0 + 1.  From 2^51, q0 is within one of its
+ * ulps (1/2 or 1) of X/c, so X - q0*|c| is exact and, with q0's own
+ * fraction (0 or 1/2), decides N.  The same integer steps as the device
+ * code, compared with the host's IEEE division.  Cases: random subnormal
+ * and tiny normal numerators against constants in [2^-100, 2^100]
+ * wherever the path applies, numerators at the top of its range (q0 from
+ * 2^51 to 2^53 - 1), exact quotients, and exact ties (X/c = k + 1/2
+ * with c = 3 * 2^j, and with c = 2^j at the top of the range).
+ * Prints "mismatches cases upper_cases". */
 #include <math.h>
 #include <stdint.h>
 #include <stdio.h>
@@ -22,13 +26,13 @@ static uint64_t bits(double d) { uint64_t u; memcpy(&u, &d, 8); return u; }
 
 static int clz64(uint64_t v) { return v ? __builtin_clzll(v) : 64; }
 
-/* the device's divu_sub: nonzero x, c in [2^-100, 2^100], |x/c| < 2^-1023 */
+/* the device's divu_sub: nonzero x, c in [2^-100, 2^100], |x/c| < 2^-1021 */
 static int applies(double x, double c) {
   const uint64_t xb = bits(x), cb = bits(c);
   const unsigned ex = (unsigned)(xb >> 52) & 0x7ffu, ec = (unsigned)(cb >> 52) & 0x7ffu;
   const uint64_t m = xb & 0x000fffffffffffffull;
   const int eff = ex != 0u ? (int)ex : 12 - clz64(m);
-  return ec - 923u <= 200u && ex < 2047u && (m | ex) != 0 && eff - (int)ec <= -1024;
+  return ec - 923u <= 200u && ex < 2047u && (m | ex) != 0 && eff - (int)ec <= -1022;
 }
 
 /* the device's scale_up<K> of a non-negative x */
@@ -45,7 +49,9 @@ static double scale_up(double x, int k) {
   return from(b);
 }
 
-/* the device's sub_quotient, step for step */
+static long upper_cases = 0;
+
+/* the device's integer-grid lanes, step for step */
 static double sub_quotient(double x, double c, double rc) {
   const uint64_t xb = bits(x), cb = bits(c);
   const double X = scale_up(from(xb & 0x7fffffffffffffffull), 1074);
@@ -59,10 +65,22 @@ static double sub_quotient(double x, double c, double rc) {
   const uint64_t n0 = e < -1 ? 0ull : (qm + (1ull << (sh - 1))) >> sh;
   const int lead = 63 - clz64(n0 | 1);
   const double nd = n0 == 0 ? 0.0 : from(((uint64_t)(lead + 1023) << 52) | ((n0 << (52 - lead)) & 0x000fffffffffffffull));
-  const double r = fma(-nd, ac, X);
+  const int upper = e >= 51;
+  const int ush = e - 52 < 11 ? e - 52 : 11;
+  const uint64_t iq = e >= 52 ? qm << ush : qm >> 1;
+  const int halfq = e == 51 && (qm & 1);
+  const uint64_t base = upper ? iq : n0;
+  upper_cases += upper;
+  const double r = fma(-(upper ? q0 : nd), ac, X);
   const uint64_t rb = bits(r), ar = rb & 0x7fffffffffffffffull, half = bits(ac) - (1ull << 52);
-  const int step = ar > half || (ar == half && (n0 & 1));
-  const uint64_t n = n0 + (step ? ((rb >> 63) ? ~0ull : 1ull) : 0ull);
+  const int rneg = (int)(rb >> 63);
+  uint64_t n;
+  if (halfq) {
+    n = base + (((!rneg && ar != 0) || (ar == 0 && (base & 1))) ? 1ull : 0ull);
+  } else {
+    const int step = ar > half || (ar == half && (base & 1));
+    n = base + (step ? (rneg ? ~0ull : 1ull) : 0ull);
+  }
   return from(n | ((xb ^ cb) & 0x8000000000000000ull));
 }
 
@@ -91,9 +109,9 @@ int main(int argc, char** argv) {
     const uint64_t sg = (rnd() & 1) << 63;
     /* subnormal numerators of every length */
     check(from(sg | ((rnd() & 0x000fffffffffffffull) >> (rnd() % 53))), c);
-    /* numerators at the top of the range: biased exponent ec - 1024 and below */
+    /* numerators at the top of the range: biased exponent ec - 1022 and below */
     {
-      const int top = ec - 1024 - (int)(rnd() % 4);
+      const int top = ec - 1022 - (int)(rnd() % 6);
       if (top >= 1) check(from(sg | ((uint64_t)top << 52) | (rnd() & 0x000fffffffffffffull)), c);
       else check(from(sg | ((rnd() & 0x000fffffffffffffull) >> (1 - top))), c);
     }
@@ -102,6 +120,21 @@ int main(int argc, char** argv) {
       const double cs = from(bits(c) & 0xfffffff000000000ull);
       const double X = (double)(rnd() % (1ull << 20)) * from(bits(fabs(cs)) & 0x7ff0000000000000ull) * 0x1p30;
       if (X > 0 && X < 0x1p52) check(from(sg | bits(ldexp(X, -1074))), from(bits(cs) & 0x7ff0000000000000ull));
+    }
+    /* q0 next to 2^53: the largest significands over the smallest */
+    {
+      const int j = (int)(rnd() % 40);
+      const double cm = from(((uint64_t)(1023 + j) << 52) | (rnd() % 64));
+      const int top = 1023 + j - 1022;
+      if (top >= 1) check(from(sg | ((uint64_t)top << 52) | (0x000fffffffffffffull - (rnd() % 64))), cm);
+    }
+    /* ties at the top: c = 2^j (j >= 1), X = (2I + 1) * 2^(j - 1), X/c = I + 1/2, I in [2^50, 2^52) */
+    {
+      const int j = 1 + (int)(rnd() % 30);
+      const uint64_t I = (1ull << 50) + (rnd() % (3ull << 50));
+      const double X = ldexp((double)(2 * I + 1), j - 1);
+      check(from(sg | bits(ldexp(X, -1074))), ldexp(1.0, j));
+      check(from(sg | bits(ldexp(X, -1074))), -ldexp(1.0, j));
     }
     /* ties: c = 3 * 2^j (j >= 1), X = (2k + 1) * 3 * 2^(j - 1), X/c = k + 1/2 */
     {
@@ -114,6 +147,6 @@ int main(int argc, char** argv) {
       check(from(sg | bits(ldexp(X - 1.0, -1074))), ct);
     }
   }
-  printf("%ld %ld\n", bad, cases);
+  printf("%ld %ld %ld\n", bad, cases, upper_cases);
   return 0;
 }

@@ -2,7 +2,7 @@
 (division by a grid-independent constant through its host reciprocal, a
 quotient through a shared reciprocal, both with their last rounding step on
 the integer pipe, a multiply-add by a power of two, the comparisons on the
-integer pipe, 1 - x on the integer pipe, quotients below 2^-1023 rounded on
+integer pipe, 1 - x on the integer pipe, quotients below 2^-1021 rounded on
 the integer grid)
 against the reference's separately rounded IEEE operations: bit for bit on
 2^28 operands per seed wherever their range flag stays set; the operands
@@ -44,7 +44,7 @@ def test_exact_forms_match_ieee(lib, seed):
     # 1 - x, warp by warp and its integer form lane by lane
     assert out[9] == 0, ("one_minus mismatches", out[9])
     assert 0.4 * n < out[10] < n, out[10]
-    # quotients below 2^-1023 rounded on the integer grid, lane by lane (the
+    # quotients below 2^-1021 rounded on the integer grid, lane by lane (the
     # warp-level division above also meets them mixed with the other paths)
     assert out[11] == 0, ("subnormal quotient mismatches", out[11])
     assert out[12] > 0.02 * n, out[12]

@@ -52,14 +52,16 @@ def test_one_minus_integer_pipe(tmp_path):
 
 
 def test_subnormal_quotient_integer_grid(tmp_path):
-    """Quotients below 2^-1023 by a grid-independent constant, rounded on the
-    integer grid of the subnormals (N = RN(X/c) for X = |x| * 2^1074, from
-    RN(X * RN(1/c)) rounded to an integer and the exact remainder), with the
-    device's steps on the host: identical to RN(x/c) on about 9 * 10^6
-    cases, exact ties and exact quotients included."""
+    """Quotients below 2^-1021 by a grid-independent constant, rounded on the
+    integer grid of the subnormals (N = RN(X/c) for X = |x| * 2^1074: below
+    2^51 from RN(X * RN(1/c)) rounded to an integer and the exact remainder,
+    from 2^51 from that product's own remainder and fraction), with the
+    device's steps on the host: identical to RN(x/c) on about 1.5 * 10^7
+    cases, exact ties (also at the top of the range) and exact quotients
+    included."""
     exe = str(tmp_path / "subnormal_quotient_host")
     subprocess.check_call(["gcc", "-O2", "-ffp-contract=off",
                            os.path.join(HERE, "native", "subnormal_quotient_host.c"), "-o", exe, "-lm"])
-    bad, cases = map(int, subprocess.check_output([exe, "2000000"], text=True).split())
+    bad, cases, upper = map(int, subprocess.check_output([exe, "2000000"], text=True).split())
     assert bad == 0
-    assert cases > 5 * 10**6
+    assert cases > 10**7 and upper > 10**6
