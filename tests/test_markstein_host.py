@@ -65,3 +65,26 @@ def test_subnormal_quotient_integer_grid(tmp_path):
     bad, cases, upper = map(int, subprocess.check_output([exe, "2000000"], text=True).split())
     assert bad == 0
     assert cases > 10**7 and upper > 10**6
+
+
+def test_division_forms_cover_the_range():
+    """Which numerators the FP64 division by a grid-independent constant
+    leaves to the IEEE division, exponent by exponent (the device's window,
+    tiny and integer-grid tests of F64Exact::divu, restated): of the
+    numerators of exponent at most 960 whose quotient's exponent is at most
+    1000, none when the divisor lies in [2^-100, 2^40]; above 2^40, only
+    those of exponent at least -960 whose quotient lies in
+    [2^-1021, 2^-1000)."""
+    def forms(ex, eff, ec):
+        window = 63 <= ex <= 1983 and 0 <= ex - ec + 1000 <= 2000
+        tiny = ex < 63 and eff + 1021 >= ec
+        below = eff - ec <= -1022
+        return window or tiny or below
+
+    for ec in range(1023 - 100, 1023 + 101):
+        for ex in range(0, 2047):
+            for eff in (range(-51, 1) if ex == 0 else (ex,)):
+                if ex > 1983 or ex - ec > 1000 or forms(ex, eff, ec):
+                    continue
+                assert ec - 1023 > 40, (ec - 1023, ex - 1023)
+                assert ex - 1023 >= -960 and -1021 <= ex - ec <= -1001, (ec - 1023, ex - 1023)
