@@ -88,3 +88,19 @@ def test_division_forms_cover_the_range():
                     continue
                 assert ec - 1023 > 40, (ec - 1023, ex - 1023)
                 assert ex - 1023 >= -960 and -1021 <= ex - ec <= -1001, (ec - 1023, ex - 1023)
+
+
+def test_division_warp_forms(tmp_path):
+    """The division by a grid-independent constant as a warp of 32 lanes
+    takes it (the window; window or tiny numerators scaled by 2^256; those
+    or quotients below 2^-1021 on the integer grid; else the IEEE
+    division), with the device's steps on the host: every lane identical to
+    RN(x/c) on 9.6 * 10^6 lanes of warps that mix the numerator classes,
+    every form taken."""
+    exe = str(tmp_path / "divu_warp_host")
+    subprocess.check_call(["gcc", "-O2", "-ffp-contract=off", os.path.join(HERE, "native", "divu_warp_host.c"),
+                           "-o", exe, "-lm"])
+    bad, lanes, *forms = map(int, subprocess.check_output([exe, "300000"], text=True).split())
+    assert bad == 0
+    assert lanes == 300000 * 32
+    assert all(f > 10000 for f in forms), forms
