@@ -26,13 +26,16 @@ struct F64Ieee;
 // of two, a division by a grid-independent value through its host
 // reciprocal and a division through a shared reciprocal.  Each checks on the
 // integer pipe whether its operands lie in its window.  The divisions take a
-// warp-uniform branch to the IEEE division when a lane's operands do not;
+// warp-uniform branch when a lane's operands do not: the division by a
+// grid-independent value to its forms for numerators below the window
+// (divu_outside), else, like the other division, to the IEEE division;
 // the multiply-add, whose window is left only near overflow or underflow,
 // records it in the `ok` flag of the stage functor (which run() returns),
 // and a warp in which any lane's flag dropped evaluates the functor again
 // with F64Ieee, the plain separately rounded operations (eval() below).
 // Inside the windows both forms give the same bits, so the result never
-// depends on which lanes share a warp.
+// depends on which lanes share a warp.  Comparisons, |x| and 1 - x (for x
+// in [0.5, 2), else the FP64 subtraction) run on the integer pipe, exactly.
 struct F64Exact {
   using T = double;
   using U = double;   // element type of the uniform table
